@@ -1,0 +1,68 @@
+// Short on-device timing loops that give the FP64 (DFMA) and FP32 (FFMA)
+// throughput used as roofline denominators for the FP64 form.
+#include <cuda_runtime.h>
+
+#include "atrip_gb300.h"
+#include "engine.cuh"
+
+namespace {
+
+constexpr int kChains = 8;
+
+template <typename T>
+__global__ void fma_chains(T *out, int iters, T s) {
+  T acc[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) acc[c] = (T)(threadIdx.x * 1e-3 + c);
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) acc[c] = acc[c] * s + (T)1e-9;
+  T r = 0;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) r += acc[c];
+  if (r == (T)12345.678) out[0] = r;  // keeps the chains live
+}
+
+template <typename T>
+double time_fma(int sms, int iters) {
+  T *d = nullptr;
+  if (cudaMalloc(&d, 64) != cudaSuccess) return 0.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = sms * 4, threads = 256;
+  fma_chains<T><<<blocks, threads>>>(d, 16, (T)1.0000001);
+  cudaDeviceSynchronize();
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    fma_chains<T><<<blocks, threads>>>(d, iters, (T)1.0000001);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  const double flops = 2.0 * kChains * (double)iters * blocks * threads;
+  return flops / (best * 1e-3) / 1e12;
+}
+
+}  // namespace
+
+extern "C" int atrip_gpu_measure_peaks(int32_t device, double *fp64_tflops, double *fp32_tflops) {
+  atrip_gb300::clear_error();
+  if (!fp64_tflops || !fp32_tflops) {
+    atrip_gb300::set_error("null argument");
+    return ATRIP_ERR_ARGUMENT;
+  }
+  ATRIP_CUDA_TRY(cudaSetDevice(device));
+  int sms = 0;
+  ATRIP_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  *fp64_tflops = time_fma<double>(sms, 4096);
+  *fp32_tflops = time_fma<float>(sms, 16384);
+  ATRIP_CUDA_TRY(cudaGetLastError());
+  return ATRIP_OK;
+}

@@ -1,0 +1,28 @@
+// Split-precision (BF16 slices on tcgen05 tensor cores) form of the triples
+// kernel: state kept per context and the entry point used by atrip_gpu_run.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "engine.cuh"
+
+namespace atrip_gb300 {
+
+struct SplitState {
+  bool valid = false;  // pre-split operands match the uploaded tensors
+  int slices = 0;
+  void *impl = nullptr;
+};
+
+void split_invalidate(SplitState &s);
+void split_free(SplitState &s);
+
+// Runs tuples [t_begin, t_end) in the split form, writing e[t], ect[t].
+int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
+              const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,
+              int64_t t_end, double tai_sign, bool use_j, int slices,
+              unsigned long long *queue, double *e, double *ect, cudaStream_t st,
+              int64_t *launches);
+
+}  // namespace atrip_gb300

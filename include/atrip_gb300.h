@@ -1,0 +1,163 @@
+/*
+ * atrip_gb300 -- C ABI of the GB300 CCSD(T) triples engine.
+ *
+ * This is the boundary under atrip's public C++ API (atrip::Atrip::Input /
+ * Atrip::run / Atrip::Output, src/atrip/Atrip.hpp:41-140).  The header-only
+ * C++ drop-in in include/atrip/Atrip.hpp calls these entry points; a host in
+ * any language can bind them directly (plain pointers, sizes, status codes,
+ * no CUDA or torch types in any signature).
+ *
+ * One context owns one GPU's worth of state: the HBM-resident operand
+ * tensors in kernel-friendly layouts, the tuple work queue and the per-tuple
+ * energy array.  It replaces atrip's per-rank state (the static members of
+ * struct Atrip, src/atrip/Atrip.hpp:43-63), its SliceUnions
+ * (src/atrip/Atrip.cxx:277-362) and its tuple distribution
+ * (src/atrip/Tuples.hpp:49-52).  Contexts are independent; one context must
+ * not be used from two host threads at once.
+ *
+ * All input arrays are FP64 and column-major (first index fastest), i.e.
+ * exactly what CTF::Tensor::read_all returns for atrip's inputs.
+ *
+ * Every entry point returns ATRIP_OK (0) or a status below; the text of the
+ * last error on the calling thread is available from atrip_gpu_last_error().
+ */
+#ifndef ATRIP_GB300_H
+#define ATRIP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  atrip throws const char* / std::string on failure
+ * (src/atrip/Acc.hpp:16-41, src/atrip/CUDA.hpp:27-38); the C++ drop-in turns
+ * a non-zero status into a thrown std::string with atrip_gpu_last_error(). */
+enum atrip_status {
+  ATRIP_OK = 0,
+  ATRIP_ERR_ARGUMENT = 1,      /* bad pointer, size, tensor id or option   */
+  ATRIP_ERR_CUDA = 2,          /* a CUDA runtime call failed               */
+  ATRIP_ERR_OUT_OF_MEMORY = 3, /* device allocation failed                 */
+  ATRIP_ERR_STATE = 4,         /* missing input, or call out of order      */
+  ATRIP_ERR_TIMEOUT = 5,       /* a device-side bounded wait gave up       */
+  ATRIP_ERR_UNSUPPORTED = 6,   /* size or form this build does not support */
+  ATRIP_ERR_NO_DEVICE = 7      /* no usable sm_103 device                  */
+};
+
+/* Input tensors, named after atrip's Input::with_* builders
+ * (src/atrip/Atrip.hpp:72-107).  Shapes (column-major):
+ *   EPSI  (No)            EPSA  (Nv)           TAI   (Nv,No)
+ *   TABIJ (Nv,Nv,No,No)   VABIJ (Nv,Nv,No,No)  VIJKA (No,No,No,Nv)
+ *   VABCI (Nv,Nv,Nv,No)   JIJKA (No,No,No,Nv)  JABCI (Nv,Nv,Nv,No)      */
+enum atrip_tensor {
+  ATRIP_EPSI = 0,
+  ATRIP_EPSA = 1,
+  ATRIP_TAI = 2,
+  ATRIP_TABIJ = 3,
+  ATRIP_VABIJ = 4,
+  ATRIP_VIJKA = 5,
+  ATRIP_VABCI = 6,
+  ATRIP_JIJKA = 7,
+  ATRIP_JABCI = 8,
+  ATRIP_N_TENSORS = 9
+};
+
+/* Arithmetic form of the contractions. */
+enum atrip_form {
+  ATRIP_FORM_FP64 = 0,       /* FP64 throughout                               */
+  ATRIP_FORM_SPLIT_BF16 = 1, /* operands cut into BF16 slices, tensor cores,  */
+                             /* FP32 accumulation, FP64 recombination         */
+  ATRIP_FORM_AUTO = 2        /* the context's tuned choice                    */
+};
+
+typedef struct atrip_gpu_context atrip_gpu_context;
+
+typedef struct {
+  int32_t no;     /* occupied orbitals, 1 <= no <= 64   */
+  int32_t nv;     /* virtual orbitals,  1 <= nv <= 1023 */
+  int32_t device; /* CUDA device ordinal                */
+  int32_t reserved;
+} atrip_dims;
+
+/* Options of one run; mirrors the Input attributes that change results or
+ * the tuple range (src/atrip/Atrip.hpp:113-131).  Zero-initialise and set
+ * what you need. */
+typedef struct {
+  int32_t form;            /* enum atrip_form                                  */
+  int32_t slices;          /* split form: BF16 slices per operand, 2..4 (0: 3) */
+  int32_t ijkabc;          /* Input::ijkabc: negate T1, skip final negation    */
+  int32_t use_j;           /* 1: (cT) with JIJKA/JABCI when both uploaded      */
+  int64_t first_iteration; /* resume cursor (checkpoint Iteration)             */
+  int64_t max_iterations;  /* Input::max_iterations: 0 = all; else tuples      */
+                           /* first_iteration .. max_iterations inclusive      */
+  double start_energy;     /* checkpoint Energy (physical sign), added back    */
+  void *stream;            /* cudaStream_t to run on, NULL = context stream    */
+} atrip_run_options;
+
+typedef struct {
+  double energy;         /* Output::energy    (src/atrip/Atrip.hpp:134-137)   */
+  double ct_energy;      /* Output::ct_energy                                 */
+  int64_t tuples_done;   /* tuples processed in this run                      */
+  int64_t next_iteration;/* cursor after the run (for checkpoints)            */
+  double device_ms;      /* device time of the tuple loop (CUDA events)       */
+  int32_t form_used;     /* enum atrip_form actually run                      */
+  int32_t slices_used;   /* split form: slices per operand                    */
+  int64_t kernel_launches; /* kernels this library launched in the run        */
+} atrip_result;
+
+/* Create a context on dims->device.  Replaces the per-rank device setup of
+ * Atrip::run (src/atrip/Atrip.cxx:78-171) and the tuple list
+ * (src/atrip/Tuples.cxx:89-134, built once on the host, kept on device). */
+int atrip_gpu_create(const atrip_dims *dims, atrip_gpu_context **out);
+
+/* Upload one input tensor from host memory (pageable or pinned), n_elements
+ * FP64 values in column-major order.  The device copy is kept in the
+ * engine's own layout.  Replaces read_all + the SliceUnion constructors
+ * (src/atrip/Atrip.cxx:176-215, 277-362; src/atrip/Unions.hpp:77-278).     */
+int atrip_gpu_upload(atrip_gpu_context *ctx, int32_t tensor, const double *host_colmajor,
+                     int64_t n_elements);
+
+/* Same from device memory (a column-major FP64 array already in HBM). */
+int atrip_gpu_upload_device(atrip_gpu_context *ctx, int32_t tensor,
+                            const double *device_colmajor, int64_t n_elements);
+
+/* Drop an uploaded tensor (atrip's Input::delete_Vppph,
+ * src/atrip/Atrip.cxx:310, frees the caller's V_pphp after slicing). */
+int atrip_gpu_release(atrip_gpu_context *ctx, int32_t tensor);
+
+/* Run the triples loop over the tuple range selected by opts and reduce the
+ * energies.  Replaces the per-tuple loop and the final reduction of
+ * Atrip::run (src/atrip/Atrip.cxx:686-1111): doubles_contribution,
+ * singles_contribution and get_energy_{same,distinct}
+ * (src/atrip/Equations.cxx:101-238, 387-426, 455-728). Blocks until done. */
+int atrip_gpu_run(atrip_gpu_context *ctx, const atrip_run_options *opts, atrip_result *out);
+
+/* Per-tuple energies of the last run, tuple-list positions t0 .. t0+n-1
+ * (the sign atrip accumulates before its final negation). ect may be NULL. */
+int atrip_gpu_tuple_energies(atrip_gpu_context *ctx, int64_t t0, int64_t n, double *e,
+                             double *ect);
+
+/* Number of tuples for nv (src/atrip/Tuples.cxx:93) and the (a,b,c) of list
+ * position t (src/atrip/Tuples.cxx:122-134).  No context needed.           */
+int64_t atrip_gpu_n_tuples(int32_t nv);
+int atrip_gpu_tuple_at(int32_t nv, int64_t t, int32_t *a, int32_t *b, int32_t *c);
+
+/* Destroy a context and free its device memory. */
+int atrip_gpu_destroy(atrip_gpu_context *ctx);
+
+/* Text of the last failure on this host thread ("" if none). */
+const char *atrip_gpu_last_error(void);
+
+/* Library version string. */
+const char *atrip_gpu_version(void);
+
+/* Measured FP64 (DFMA) and FP32 (FFMA) throughput of the device in TFLOP/s,
+ * from a short on-device timing loop (used as roofline denominators). */
+int atrip_gpu_measure_peaks(int32_t device, double *fp64_tflops, double *fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ATRIP_GB300_H */
