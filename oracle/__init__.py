@@ -80,6 +80,13 @@ def _load():
         lib.oracle_energy_distinct.argtypes = [ctypes.c_double, ctypes.c_int] + [ctypes.c_void_p] * 3
         lib.oracle_energy_same.restype = ctypes.c_double
         lib.oracle_energy_same.argtypes = [ctypes.c_double, ctypes.c_int] + [ctypes.c_void_p] * 3
+        lib.oracle_port_prepare.restype = ctypes.c_void_p
+        lib.oracle_port_prepare.argtypes = [ctypes.POINTER(_Inputs)]
+        lib.oracle_port_run.restype = ctypes.c_int
+        lib.oracle_port_run.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.c_void_p]
+        lib.oracle_port_free.argtypes = [ctypes.c_void_p]
         _lib = lib
     return _lib
 
@@ -153,6 +160,30 @@ def run(p: Problem, ijkabc: bool = False, use_j: bool = True, threads: int = 1,
     sign = 1.0 if ijkabc else -1.0
     local = -start_energy  # src/atrip/Atrip.cxx:612-616 negates unconditionally
     return sign * (local + float(np.sum(e))), sign * (float(np.sum(ect)))
+
+
+class PreparedPort:
+    """The DGEMM-route port with its operand slices cut once, so that tuple
+    ranges can be timed without the set-up (bench.py's CPU baseline)."""
+
+    def __init__(self, p: Problem):
+        self.p = p
+        self.h = _load().oracle_port_prepare(ctypes.byref(p.c))
+
+    def run(self, t0: int, t1: int, threads: int, ijkabc: bool = False, use_j: bool = True):
+        n = t1 - t0
+        e = np.zeros(max(n, 1))
+        ect = np.zeros(max(n, 1))
+        rc = _load().oracle_port_run(self.h, t0, t1, int(ijkabc), int(use_j), threads,
+                                     e.ctypes.data, ect.ctypes.data)
+        if rc != 0:
+            raise ValueError("oracle_port_run rejected its arguments")
+        return e[:n], ect[:n]
+
+    def close(self):
+        if self.h:
+            _load().oracle_port_free(self.h)
+            self.h = None
 
 
 def tuple_arrays(p: Problem, a: int, b: int, c: int, ijkabc: bool = False):

@@ -447,6 +447,54 @@ int oracle_tuple_energies(const oracle_inputs *in, int64_t t0, int64_t t1, int i
   return 0;
 }
 
+/* Prepared DGEMM-route port: slices cut once, then timed tuple ranges
+ * (bench.py's CPU baseline times oracle_port_run only). */
+typedef struct {
+  oracle_inputs in;
+  port_slices s;
+  int32_t *abc;
+} oracle_port;
+
+void *oracle_port_prepare(const oracle_inputs *in) {
+  oracle_port *p = (oracle_port *)calloc(1, sizeof(oracle_port));
+  p->in = *in;
+  cut_slices(in, &p->s);
+  const int64_t n = oracle_n_tuples(in->Nv);
+  p->abc = (int32_t *)malloc(sizeof(int32_t) * 3 * (n > 0 ? n : 1));
+  oracle_tuple_list(in->Nv, p->abc);
+  return p;
+}
+
+int oracle_port_run(void *h, int64_t t0, int64_t t1, int ijkabc, int use_j, int nthreads,
+                    double *e, double *ect) {
+  oracle_port *p = (oracle_port *)h;
+  const int64_t n = oracle_n_tuples(p->in.Nv);
+  if (!p || t0 < 0 || t1 > n || t0 > t1 || nthreads < 1) return 1;
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+  worker_args *args = (worker_args *)malloc(sizeof(worker_args) * nthreads);
+  const int64_t per = (t1 - t0 + nthreads - 1) / nthreads;
+  for (int r = 0; r < nthreads; ++r) {
+    worker_args w = {&p->in, &p->s, p->abc, t0 + r * per, t0 + (r + 1) * per, ijkabc, use_j, 1,
+                     e - t0, ect - t0};
+    if (w.t0 > t1) w.t0 = t1;
+    if (w.t1 > t1) w.t1 = t1;
+    args[r] = w;
+    pthread_create(&th[r], 0, worker, &args[r]);
+  }
+  for (int r = 0; r < nthreads; ++r) pthread_join(th[r], 0);
+  free(th);
+  free(args);
+  return 0;
+}
+
+void oracle_port_free(void *h) {
+  oracle_port *p = (oracle_port *)h;
+  if (!p) return;
+  free_slices(&p->s);
+  free(p->abc);
+  free(p);
+}
+
 /* Tijk and Zijk of one tuple through the naive route (element-wise checks). */
 int oracle_tuple_arrays(const oracle_inputs *in, int a, int b, int c, int ijkabc, double *Tijk,
                         double *Zijk) {
