@@ -1,0 +1,51 @@
+"""The C-ABI library loads without a GPU and exports every entry point that
+include/*.h declares (no compute calls are made)."""
+import ctypes
+import glob
+import os
+import re
+
+from atrip_gb300 import _build, capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(atrip_gpu_\w+)\s*\(", text):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    _build.build()
+    lib = ctypes.CDLL(_build.LIB)
+    names = declared_symbols()
+    assert len(names) >= 12
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(capi.EXPORTED) <= names
+
+
+def test_pure_host_entry_points():
+    lib = capi.load()
+    assert lib.atrip_gpu_version().startswith(b"atrip_gb300")
+    assert capi.n_tuples(1) == 0 and capi.n_tuples(2) == 2 and capi.n_tuples(40) == 11440
+    import oracle
+    for nv in (2, 3, 9, 40):
+        lst = oracle.tuple_list(nv)
+        for t in range(len(lst)):
+            assert tuple(lst[t]) == capi.tuple_at(nv, t)
+
+
+def test_errors_without_gpu_are_status_codes():
+    lib = capi.load()
+    ctx = ctypes.c_void_p()
+    rc = lib.atrip_gpu_create(ctypes.byref(capi.Dims(0, 10, 0, 0)), ctypes.byref(ctx))
+    assert rc == capi.ERR_UNSUPPORTED
+    assert b"No must be" in lib.atrip_gpu_last_error()
+    rc = lib.atrip_gpu_tuple_at(10, 10 ** 6, *(ctypes.byref(ctypes.c_int32()) for _ in range(3)))
+    assert rc == capi.ERR_ARGUMENT
