@@ -25,6 +25,7 @@ EXPORTED = [
     "atrip_gpu_create", "atrip_gpu_upload", "atrip_gpu_upload_device", "atrip_gpu_release",
     "atrip_gpu_run", "atrip_gpu_tuple_energies", "atrip_gpu_n_tuples", "atrip_gpu_tuple_at",
     "atrip_gpu_destroy", "atrip_gpu_last_error", "atrip_gpu_version", "atrip_gpu_measure_peaks",
+    "atrip_gpu_run_fp64_noalloc",
 ]
 
 
@@ -44,6 +45,12 @@ class RunOptions(ctypes.Structure):
                 ("use_j", ctypes.c_int32), ("first_iteration", ctypes.c_int64),
                 ("max_iterations", ctypes.c_int64), ("start_energy", ctypes.c_double),
                 ("stream", ctypes.c_void_p)]
+
+
+class DeviceInputs(ctypes.Structure):
+    """atrip_device_inputs: device pointers to column-major FP64 tensors."""
+    _fields_ = [(n, ctypes.c_void_p) for n in
+                ("epsi", "epsa", "tai", "tabij", "vabij", "vijka", "vabci", "jijka", "jabci")]
 
 
 class Result(ctypes.Structure):
@@ -86,6 +93,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.atrip_gpu_version.restype = ctypes.c_char_p
     lib.atrip_gpu_measure_peaks.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_double)]
+    lib.atrip_gpu_run_fp64_noalloc.argtypes = [
+        ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(DeviceInputs), ctypes.c_int64,
+        ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_void_p]
     for name in EXPORTED:
         if name not in ("atrip_gpu_n_tuples", "atrip_gpu_last_error", "atrip_gpu_version"):
             getattr(lib, name).restype = ctypes.c_int

@@ -156,6 +156,45 @@ const char *atrip_gpu_version(void);
  * from a short on-device timing loop (used as roofline denominators). */
 int atrip_gpu_measure_peaks(int32_t device, double *fp64_tflops, double *fp32_tflops);
 
+/* ---------------------------------------------------------------------
+ * No-allocation variant (no counterpart in the reference).
+ *
+ * For hosts that cannot call cudaMalloc: codes whose own pool allocator
+ * owns all device memory, or frameworks that forbid device allocations on
+ * their worker threads because cudaMalloc/cudaFree synchronise the device.
+ * The caller passes device pointers to its column-major FP64 inputs (the
+ * layout CTF's read_all returns) and to its outputs; the FP64 triples loop
+ * runs without allocating anything.
+ *
+ * Scratch (work-queue cursor, per-CTA W buffers, reduction partials) lives
+ * in one fixed 32 MiB __device__ array inside the library.  Every GPU that
+ * loads the library holds that array until the process exits.  All calls
+ * share it: each call clears what must start at zero, and calls whose
+ * kernels overlap on the GPU (other streams, other host threads) race on it,
+ * so serialise them.  The first call on a device looks the array's device
+ * address up once (cudaGetSymbolAddress, with that device current); make
+ * that first call before any stream capture.  Limits: 1 <= No <= 64 (2 No^3
+ * doubles of W per CTA must fit in the array), 1 <= Nv <= 1023.
+ *
+ * Tuples first_iteration .. max_iterations (inclusive; 0 = all) are run on
+ * the current device, in `stream` (NULL = default stream); the call returns
+ * after queueing the work.  Outputs (device memory, valid once the stream
+ * has reached them):
+ *   tuple_e[t - t0], tuple_ect[t - t0]  per-tuple energies, t0 = first tuple
+ *                                       run (n = number of tuples in range)
+ *   energies[0], energies[1]            energy and ct_energy of the range,
+ *                                       final sign applied as in
+ *                                       atrip_gpu_run (no checkpoint energy)
+ * jijka/jabci may be NULL (then ct_energy == energy).                      */
+typedef struct {
+  const double *epsi, *epsa, *tai, *tabij, *vabij, *vijka, *vabci, *jijka, *jabci;
+} atrip_device_inputs;
+
+int atrip_gpu_run_fp64_noalloc(int32_t no, int32_t nv, const atrip_device_inputs *in,
+                               int64_t first_iteration, int64_t max_iterations, int32_t ijkabc,
+                               int32_t use_j, double *tuple_e, double *tuple_ect,
+                               double *energies, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
