@@ -1,16 +1,802 @@
-// Split-precision form (BF16 slices, tcgen05) -- entry points.
+// Split-precision form of the triples kernel: FP64 operands cut into BF16
+// "digit" slices, contractions on the tcgen05 tensor cores with FP32
+// accumulation in TMEM, exact integer / FP64 recombination.
+//
+// Splitting (done once per upload, in FP64).  With one power-of-two scale per
+// tensor (2^eT for T, 2^eV shared by V_pphp and V_hhhp so that particle and
+// hole products land on the same grid), an element x is written as
+//     x = 2^(e-7) * sum_p q_p 2^(-8p),   q_p integer, |q_p| <= 128,
+// q_p = rint of the running remainder.  Each q_p is exact in BF16, every
+// product q_p q'_q is an integer below 2^14, and a dot product of up to 1024
+// such terms is an integer below 2^24, hence exact in the FP32 accumulator.
+// Products are grouped by level L = p + q (pairs with L < S are kept; S =
+// slices); level 0 is exact, levels >= 1 carry a 2^-8L smaller weight.
+//
+// Contraction structure.  The six fused particle+hole terms of the FP64
+// form (src/atrip/Equations.cxx:455-728) pair up by output column index:
+// term t and its partner share the column index and run over the same pair
+// of row indices in opposite order.  Loading the partner's A rows from a
+// transposed copy makes both land in the same TMEM rows, so each pair is one
+// K-concatenated GEMM (K = 2 (Nv + No)) into one accumulator:
+//   G0  rows (i,j), column k:  T_a/Vh_b (natural)  + T_b/Vh_a (transposed)
+//   G1  rows (i,k), column j:  T_a/Vh_c            + T_c/Vh_a
+//   G2  rows (j,k), column i:  T_b/Vh_c            + T_c/Vh_b
+// and W[i,j,k] = G0 + G1 + G2, accumulated per element as an exact int32
+// (level 0) plus an FP32 remainder (levels >= 1) in shared memory.  The
+// energy loop converts W = unit * (int + rem) to FP64 and evaluates Zijk and
+// get_energy_{distinct,same} (src/atrip/Equations.cxx:101-238, 387-426) in
+// FP64.
+//
+// Kernel roles (256 threads, one persistent CTA per SM):
+//   warp 0      TMA producer: A slice tile + the B slice tiles it pairs with
+//   warp 1      TMEM owner and single-thread tcgen05.mma issuer
+//   warps 4..7  epilogue: tcgen05.ld of the level accumulators, scatter-add
+//               into W at the group's index permutation
+//   all warps   energy loop and reduction at the end of each tuple
+// Smem ring of operand stages (full/empty mbarriers), two TMEM accumulator
+// buffers (full/empty mbarriers); every wait is bounded (sm100.cuh).
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "engine.cuh"
+#include "sm100.cuh"
 #include "split.cuh"
 
 namespace atrip_gb300 {
+namespace {
+
+using namespace sm100;
+
+constexpr int kThreads = 256;
+constexpr int kMaxStages = 6;
+constexpr int kSmemLimit = 232448;  // opt-in dynamic shared memory per block
+constexpr int kTailBytes = 256 + 3 * 64 * 8 + 16 * 8;  // barriers, t1 rows, reduction
+constexpr int kKChunk = 64;              // BF16 elements per 128-byte row
+constexpr int kATileBytes = 128 * 128;   // 128 rows x 128 B
+constexpr int kHoleK = 64;               // hole K (L) padded to one chunk
+
+enum : int {
+  kErrTimeoutFull = 1,
+  kErrTimeoutEmpty = 2,
+  kErrTimeoutAccFull = 3,
+  kErrTimeoutAccEmpty = 4
+};
+
+struct SplitMaps {
+  CUtensorMap TaN, TaT, VhN, VhT, Vp, TpN, TpT;
+};
+
+struct SplitArgs {
+  int No, Nv, jt, ntiles, kch;  // j per M-tile, M-tiles per group, K chunks of Nv
+  int nstages;                 // operand ring depth
+  const double *epsi, *epsa, *tai, *Vhh;
+  const uint32_t *tuples, *triples;
+  int n_triples;
+  int64_t t_begin, t_end;
+  unsigned long long *queue;
+  double tai_sign, unit;
+  double *e, *ect;
+  int *status;
+  float *wglobal;  // per-CTA W (int32 + float) when it does not fit in smem
+};
+
+// ------------------------------------------------------------------ prep
+
+__global__ void absmax_kernel(const double *__restrict__ x, int64_t n,
+                              unsigned long long *__restrict__ out) {
+  double m = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    m = fmax(m, fabs(x[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// dst[s][R][k] (pitch Kp, BF16) = sign * digit_s(src(R, k) * scale) for
+// k < K, 0 for K <= k < Kp.  Row R = (o * n1 + r1) * n2 + r2.
+struct SliceJob {
+  const double *src;
+  __nv_bfloat16 *dst;
+  int64_t nrows, n1, n2, so, s1, s2, sk;
+  int K, Kp, S;
+  double scale, sign;
+};
+
+__global__ void slice_kernel(SliceJob j) {
+  const int64_t total = j.nrows * j.Kp;
+  const int64_t plane = total;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t R = idx / j.Kp;
+    const int k = (int)(idx - R * j.Kp);
+    double y = 0.0;
+    if (k < j.K) {
+      const int64_t r2 = R % j.n2, t = R / j.n2, r1 = t % j.n1, o = t / j.n1;
+      y = j.src[o * j.so + r1 * j.s1 + r2 * j.s2 + k * j.sk] * j.scale;
+    }
+    for (int s = 0; s < j.S; ++s) {
+      const double q = rint(y);
+      j.dst[s * plane + idx] = __double2bfloat16(j.sign * q);
+      y = (y - q) * 256.0;
+    }
+  }
+}
+
+// --------------------------------------------------------------- kernel
+
+__device__ __forceinline__ void named_bar_sync(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+struct Part {
+  const CUtensorMap *amap, *bmap;
+  int ax, bz, by;  // A: tensor index (x or w); B: (z, y) or (v, u)
+  bool particle;
+};
+
+// Operand sources of group g, part pt (0 nat particle, 1 nat hole,
+// 2 transposed particle, 3 transposed hole) for tuple (a,b,c).
+__device__ __forceinline__ Part part_of(const SplitMaps &m, int g, int pt, int a, int b, int c) {
+  // per group: natural (x, w, (y,z), hole (u,v), holeT), transposed likewise
+  int x, w, y, z, u, v, holeT;
+  const bool tr = pt >= 2;
+  if (g == 0) {
+    if (!tr) { x = a; w = b; y = b; z = c; u = a; v = c; holeT = 0; }
+    else     { x = b; w = a; y = a; z = c; u = b; v = c; holeT = 0; }
+  } else if (g == 1) {
+    if (!tr) { x = a; w = c; y = c; z = b; u = a; v = b; holeT = 0; }
+    else     { x = c; w = a; y = a; z = b; u = b; v = c; holeT = 1; }
+  } else {
+    if (!tr) { x = b; w = c; y = c; z = a; u = a; v = b; holeT = 1; }
+    else     { x = c; w = b; y = b; z = a; u = a; v = c; holeT = 1; }
+  }
+  Part p;
+  p.particle = (pt & 1) == 0;
+  if (p.particle) {
+    p.amap = tr ? &m.TaT : &m.TaN;
+    p.ax = x;
+    p.bmap = &m.Vp;
+    p.bz = z;
+    p.by = y;
+  } else {
+    p.amap = tr ? &m.VhT : &m.VhN;
+    p.ax = w;
+    p.bmap = holeT ? &m.TpT : &m.TpN;
+    p.bz = v;
+    p.by = u;
+  }
+  return p;
+}
+
+template <int S, int NP, bool WSMEM, bool SPLIT0>
+struct KernelShape {
+  static constexpr int kNacc = S + (SPLIT0 ? 1 : 0);
+  static constexpr int kBufCols = kNacc * NP;
+  static constexpr int kNbuf = (2 * kBufCols <= 512) ? 2 : 1;
+  static constexpr int kCols = kNbuf * kBufCols;
+  static constexpr int kAllocCols = kCols <= 32 ? 32 : kCols <= 64 ? 64 : kCols <= 128 ? 128
+                                    : kCols <= 256 ? 256 : 512;
+  static constexpr int kBTile = NP * 128;
+  static constexpr int kStageBytes = kATileBytes + S * kBTile;
+};
+
+template <int S, int NP, bool WSMEM, bool SPLIT0>
+__global__ void __launch_bounds__(kThreads, 1)
+    triples_split_kernel(const __grid_constant__ SplitMaps maps, const SplitArgs g) {
+  using K = KernelShape<S, NP, WSMEM, SPLIT0>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char *smem = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char *ring = smem;
+  const int No = g.No, No3 = No * No * No;
+  int32_t *WI;
+  float *WF;
+  const int kStages = g.nstages;
+  unsigned char *tail = ring + kStages * K::kStageBytes;
+  if (WSMEM) {
+    WI = reinterpret_cast<int32_t *>(tail);
+    WF = reinterpret_cast<float *>(tail + sizeof(int32_t) * No3);
+    tail += 2 * sizeof(int32_t) * ((No3 + 31) & ~31);
+  } else {
+    WI = reinterpret_cast<int32_t *>(g.wglobal + (size_t)blockIdx.x * 2 * No3);
+    WF = g.wglobal + (size_t)blockIdx.x * 2 * No3 + No3;
+  }
+  uint64_t *full = reinterpret_cast<uint64_t *>(tail);
+  uint64_t *empty = full + kStages;
+  uint64_t *accf = empty + kStages;
+  uint64_t *acce = accf + 2;
+  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(acce + 2);
+  int *slot_holder = reinterpret_cast<int *>(tmem_holder + 1);
+  double *ta = reinterpret_cast<double *>(tail + 256);
+  double *tb = ta + 64;
+  double *tc = tb + 64;
+  double *red = tc + 64;  // [8][2]
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 128);
+    }
+    fence_mbar_init();
+    prefetch_tensormap(&maps.TaN);
+    prefetch_tensormap(&maps.TaT);
+    prefetch_tensormap(&maps.VhN);
+    prefetch_tensormap(&maps.VhT);
+    prefetch_tensormap(&maps.Vp);
+    prefetch_tensormap(&maps.TpN);
+    prefetch_tensormap(&maps.TpT);
+  }
+  // rows of the A stage tiles past No*jt are never written by TMA: zero them
+  for (int i = threadIdx.x; i < kStages * K::kStageBytes / 16; i += kThreads)
+    reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
+  if (warp == 1) {
+    tmem_alloc(tmem_holder, K::kAllocCols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+
+  const uint32_t idesc = idesc_bf16_f32(128, NP);
+  const int jt = g.jt, ntiles = g.ntiles, kch = g.kch;
+  const int a_bytes = 128 * No * jt;  // full A box, out-of-range rows included
+  // role-local pipeline counters (persist across tuples)
+  uint32_t unit_count = 0, item_count = 0;
+  bool alive = true;
+
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const unsigned long long q = atomicAdd(g.queue, 1ull);
+      const bool stop = q >= (unsigned long long)(g.t_end - g.t_begin) ||
+                        *reinterpret_cast<volatile int *>(g.status) != 0;
+      *slot_holder = stop ? -1 : (int)q;
+    }
+    __syncthreads();
+    const int slot = *slot_holder;
+    if (slot < 0) break;
+    const int64_t t = g.t_begin + slot;
+    const uint32_t pk = g.tuples[t];
+    const int a = pk & 0x3ff, b = (pk >> 10) & 0x3ff, c = (pk >> 20) & 0x3ff;
+    for (int i = threadIdx.x; i < No3; i += kThreads) {
+      WI[i] = 0;
+      WF[i] = 0.f;
+    }
+    if (threadIdx.x < No) {
+      const int i = threadIdx.x;
+      ta[i] = g.tai_sign * g.tai[a + i * g.Nv];
+      tb[i] = g.tai_sign * g.tai[b + i * g.Nv];
+      tc[i] = g.tai_sign * g.tai[c + i * g.Nv];
+    }
+    __syncthreads();
+
+    if (warp == 0) {
+      // ---------------------------------------------------- TMA producer
+      if (lane == 0 && alive) {
+        for (int grp = 0; grp < 3 && alive; ++grp)
+          for (int mt = 0; mt < ntiles && alive; ++mt) {
+            const int j0 = mt * jt;
+            for (int pt = 0; pt < 4 && alive; ++pt) {
+              const Part p = part_of(maps, grp, pt, a, b, c);
+              const int nch = p.particle ? kch : 1;
+              for (int ch = 0; ch < nch && alive; ++ch)
+                for (int sa = 0; sa < S; ++sa) {
+                  const int st = unit_count % kStages;
+                  const uint32_t use = unit_count / kStages;
+                  if (use > 0 && !mbar_wait(&empty[st], (use - 1) & 1, g.status, kErrTimeoutEmpty)) {
+                    alive = false;
+                    break;
+                  }
+                  unsigned char *sbase = ring + st * K::kStageBytes;
+                  const int nb = S - sa;
+                  mbar_arrive_expect_tx(&full[st], a_bytes + nb * NP * 128);
+                  tma_load_5d(sbase, p.amap, &full[st], ch * kKChunk, 0, j0, p.ax, sa);
+                  for (int sb = 0; sb < nb; ++sb)
+                    tma_load_5d(sbase + kATileBytes + sb * K::kBTile, p.bmap, &full[st],
+                                ch * kKChunk, 0, p.bz, p.by, sb);
+                  ++unit_count;
+                }
+            }
+          }
+      }
+    } else if (warp == 1) {
+      // ------------------------------------------------------ MMA issuer
+      if (lane == 0 && alive) {
+        for (int it = 0; it < 3 * ntiles && alive; ++it) {
+          const int buf = item_count % K::kNbuf;
+          const uint32_t use = item_count / K::kNbuf;
+          if (use > 0 && !mbar_wait(&acce[buf], (use - 1) & 1, g.status, kErrTimeoutAccEmpty)) {
+            alive = false;
+            break;
+          }
+          tc_fence_after();
+          bool fresh[K::kNacc];
+#pragma unroll
+          for (int q = 0; q < K::kNacc; ++q) fresh[q] = true;
+          const uint32_t dbase = tmem + buf * K::kBufCols;
+          for (int pt = 0; pt < 4 && alive; ++pt) {
+            const int nch = (pt & 1) == 0 ? kch : 1;
+            for (int ch = 0; ch < nch && alive; ++ch)
+              for (int sa = 0; sa < S; ++sa) {
+                const int st = unit_count % kStages;
+                const uint32_t use_s = unit_count / kStages;
+                if (!mbar_wait(&full[st], use_s & 1, g.status, kErrTimeoutFull)) {
+                  alive = false;
+                  break;
+                }
+                tc_fence_after();
+                const uint32_t sbase = smem_u32(ring + st * K::kStageBytes);
+                const uint64_t adesc = sdesc_sw128(sbase);
+#pragma unroll
+                for (int sb = 0; sb < S; ++sb) {
+                  if (sb < S - sa) {
+                    const int level = sa + sb;
+                    const int acc = (SPLIT0 && level == 0 && pt >= 2) ? S : level;
+                    const uint64_t bdesc = sdesc_sw128(sbase + kATileBytes + sb * K::kBTile);
+#pragma unroll
+                    for (int kk = 0; kk < kKChunk / 16; ++kk)
+                      mma_bf16(dbase + acc * NP, adesc + 2 * kk, bdesc + 2 * kk, idesc,
+                               (fresh[acc] && kk == 0) ? 0u : 1u);
+                    fresh[acc] = false;
+                  }
+                }
+                mma_commit(&empty[st]);
+                ++unit_count;
+              }
+          }
+          mma_commit(&accf[buf]);
+          ++item_count;
+        }
+      }
+    } else if (warp >= 4) {
+      // -------------------------------------------------------- epilogue
+      const int quarter = warp - 4;
+      const int l = quarter * 32 + lane;
+      for (int it = 0; it < 3 * ntiles; ++it) {
+        const int grp = it / ntiles, mt = it % ntiles;
+        const int buf = item_count % K::kNbuf;
+        const uint32_t use = item_count / K::kNbuf;
+        bool ok = alive && mbar_wait(&accf[buf], use & 1, g.status, kErrTimeoutAccFull);
+        // the whole warp takes part in tcgen05.ld, so agree on ok; a failed
+        // wait skips the loads but still meets the named barrier below, so
+        // the four epilogue warps always execute the same barriers
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) alive = false;
+        tc_fence_after();
+        const int j0 = mt * jt;
+        const int rows = No * min(jt, No - j0);
+        const bool valid = l < rows;
+        const int f = l % No, sl = j0 + l / No;
+        const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + buf * K::kBufCols;
+        for (int c0 = 0; c0 < NP && ok; c0 += 16) {
+          float v[K::kNacc][16];
+#pragma unroll
+          for (int q = 0; q < K::kNacc; ++q) tmem_ld16(tbase + q * NP + c0, v[q]);
+          tmem_wait_ld();
+          if (valid) {
+#pragma unroll
+            for (int cc = 0; cc < 16; ++cc) {
+              const int col = c0 + cc;
+              if (col < No) {
+                int i, jj, k;
+                if (grp == 0) { i = f; jj = sl; k = col; }
+                else if (grp == 1) { i = f; k = sl; jj = col; }
+                else { jj = f; k = sl; i = col; }
+                const int idx = i + No * (jj + No * k);
+                int lev0 = __float2int_rn(v[0][cc]);
+                if (SPLIT0) lev0 += __float2int_rn(v[S][cc]);
+                float rest = 0.f;
+#pragma unroll
+                for (int q = S - 1; q >= 1; --q) rest = rest * (1.f / 256.f) + v[q][cc];
+                rest *= (1.f / 256.f);
+                WI[idx] += lev0;
+                WF[idx] += rest;
+              }
+            }
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(&acce[buf]);
+        named_bar_sync(1, 128);
+        ++item_count;
+      }
+    }
+    __syncwarp();
+    __syncthreads();
+    {
+      int bad = *reinterpret_cast<volatile int *>(g.status) != 0;
+      if (bad) alive = false;
+    }
+
+    // ---------------------------------------------------------- energy
+    int cls = 0;  // src/atrip/Atrip.cxx:640-642
+    if (a == b) cls++;
+    if (b == c) cls--;
+    const bool distinct = cls == 0;
+    const double epsabc = g.epsa[a] + g.epsa[b] + g.epsa[c];
+    const int64_t Nv = g.Nv, No2 = (int64_t)No * No;
+    const double *Vbc = g.Vhh + ((int64_t)b * Nv + c) * No2;
+    const double *Vac = g.Vhh + ((int64_t)a * Nv + c) * No2;
+    const double *Vab = g.Vhh + ((int64_t)a * Nv + b) * No2;
+    const double unit = g.unit;
+    auto W = [&](int i, int j, int k) {
+      const int idx = i + No * (j + No * k);
+      return unit * ((double)WI[idx] + (double)WF[idx]);
+    };
+    auto Zv = [&](int i, int j, int k) {
+      double z = W(i, j, k);
+      z += ta[i] * Vbc[j + k * No];
+      z += tb[j] * Vac[i + k * No];
+      z += tc[k] * Vab[i + j * No];
+      return z;
+    };
+    double sum = 0.0;
+    for (int n = threadIdx.x; n < g.n_triples; n += kThreads) {
+      const uint32_t tp = g.triples[n];
+      const int i = tp & 0xff, j = (tp >> 8) & 0xff, k = (tp >> 16) & 0xff;
+      const double facjk = j == k ? 0.5 : 1.0, facij = i == j ? 0.5 : 1.0;
+      const double denominator = epsabc - ((g.epsi[i] + g.epsi[j]) + g.epsi[k]);
+      double value;
+      if (distinct) {
+        const double U = Zv(i, j, k), V = Zv(i, k, j), Wv = Zv(j, i, k), X = Zv(j, k, i),
+                     Y = Zv(k, i, j), Z = Zv(k, j, i);
+        const double A = W(i, j, k), B = W(i, k, j), C = W(j, i, k), D = W(j, k, i),
+                     E = W(k, i, j), F = W(k, j, i);
+        const double UXY = U + (X + Y), VWZ = V + (Wv + Z), ADE = A + (D + E), BCF = B + (C + F);
+        const double first = A * U + (B * V + (C * Wv + (D * X + (E * Y + F * Z))));
+        value = 3.0 * first + ((UXY - 2.0 * VWZ) * ADE + (VWZ - 2.0 * UXY) * BCF);
+      } else {
+        const double U = Zv(i, j, k), V = Zv(j, k, i), Wv = Zv(k, i, j);
+        const double A = W(i, j, k), B = W(j, k, i), C = W(k, i, j);
+        value = 3.0 * ((A * U + B * V) + C * Wv) - (A + (B + C)) * (U + (V + Wv));
+      }
+      sum += (2.0 * value / denominator) * (facjk * facij);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) red[warp] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double e = 0.0;
+      for (int w = 0; w < kThreads / 32; ++w) e += red[w];
+      g.e[t] = e;
+      g.ect[t] = e;
+    }
+    __syncthreads();
+  }
+
+  // Leave only after every tcgen05 op of this CTA has completed.
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tmem, K::kAllocCols);
+}
+
+// ------------------------------------------------------------------ host
+
+struct SplitImpl {
+  int S = 0, No = 0, Nv = 0, Ep = 0;
+  __nv_bfloat16 *TaS = nullptr, *TaST = nullptr, *VhS = nullptr, *VhST = nullptr,
+                *VpS = nullptr, *TpS = nullptr, *TpTS = nullptr;
+  double unit = 1.0;
+  float *wglobal = nullptr;
+  size_t wglobal_floats = 0;
+  int *d_status = nullptr;
+  SplitMaps maps;
+};
+
+void free_impl(SplitImpl *p) {
+  if (!p) return;
+  cudaFree(p->TaS);
+  cudaFree(p->TaST);
+  cudaFree(p->VhS);
+  cudaFree(p->VhST);
+  cudaFree(p->VpS);
+  cudaFree(p->TpS);
+  cudaFree(p->TpTS);
+  cudaFree(p->wglobal);
+  cudaFree(p->d_status);
+  delete p;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 5-D BF16 tensor map: dims[0] fastest (K, padded), 128-byte swizzle.
+int make_map(CUtensorMap *m, const void *base, const uint64_t dims[5], const uint32_t box[5]) {
+  auto fn = encode_fn();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled not available from the driver");
+    return ATRIP_ERR_CUDA;
+  }
+  uint64_t strides[4];
+  uint64_t s = dims[0] * 2;
+  for (int i = 0; i < 4; ++i) {
+    strides[i] = s;
+    s *= dims[i + 1];
+  }
+  const uint32_t estr[5] = {1, 1, 1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed with CUresult " + std::to_string((int)r));
+    return ATRIP_ERR_CUDA;
+  }
+  return ATRIP_OK;
+}
+
+int exponent_of(double maxabs) {
+  if (!(maxabs > 0.0)) return 0;
+  return std::ilogb(maxabs) + 1;  // maxabs < 2^e
+}
+
+int absmax(const double *x, int64_t n, unsigned long long *d_tmp, cudaStream_t st, double *out) {
+  ATRIP_CUDA_TRY(cudaMemsetAsync(d_tmp, 0, sizeof(unsigned long long), st));
+  if (n > 0) {
+    absmax_kernel<<<152 * 8, 256, 0, st>>>(x, n, d_tmp);
+    ATRIP_CUDA_TRY(cudaGetLastError());
+  }
+  unsigned long long h = 0;
+  ATRIP_CUDA_TRY(cudaMemcpyAsync(&h, d_tmp, sizeof(h), cudaMemcpyDeviceToHost, st));
+  ATRIP_CUDA_TRY(cudaStreamSynchronize(st));
+  double v;
+  std::memcpy(&v, &h, sizeof(v));
+  *out = v;
+  return ATRIP_OK;
+}
+
+int run_slices(SliceJob j, cudaStream_t st) {
+  int64_t blocks = (j.nrows * j.Kp + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (blocks < 1) blocks = 1;
+  slice_kernel<<<(int)blocks, 256, 0, st>>>(j);
+  return cudaGetLastError() == cudaSuccess ? ATRIP_OK : ATRIP_ERR_CUDA;
+}
+
+int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, cudaStream_t st,
+            int64_t *launches) {
+  p->S = S;
+  p->No = No;
+  p->Nv = Nv;
+  p->Ep = (Nv + kKChunk - 1) / kKChunk * kKChunk;
+  const int64_t No2 = (int64_t)No * No, Ep = p->Ep;
+  unsigned long long *d_tmp = nullptr;
+  ATRIP_CUDA_TRY(cudaMalloc(&d_tmp, sizeof(unsigned long long)));
+  double mT = 0, mVp = 0, mVh = 0;
+  int rc = absmax(dt.Ta, (int64_t)Nv * No2 * Nv, d_tmp, st, &mT);
+  if (rc == ATRIP_OK) rc = absmax(dt.Vpt, (int64_t)Nv * Nv * No * Nv, d_tmp, st, &mVp);
+  if (rc == ATRIP_OK) rc = absmax(dt.Vht, (int64_t)Nv * No2 * No, d_tmp, st, &mVh);
+  cudaFree(d_tmp);
+  if (rc != ATRIP_OK) return rc;
+  *launches += 3;
+  const int eT = exponent_of(mT), eV = exponent_of(mVp > mVh ? mVp : mVh);
+  p->unit = std::ldexp(1.0, eT + eV - 14);
+  const double sT = std::ldexp(1.0, 7 - eT), sV = std::ldexp(1.0, 7 - eV);
+
+  const size_t nTa = (size_t)S * Nv * No2 * Ep, nVh = (size_t)S * Nv * No2 * kHoleK,
+               nVp = (size_t)S * Nv * Nv * No * Ep, nTp = (size_t)S * Nv * Nv * No * kHoleK;
+  ATRIP_CUDA_TRY(cudaMalloc(&p->TaS, 2 * nTa));
+  ATRIP_CUDA_TRY(cudaMalloc(&p->TaST, 2 * nTa));
+  ATRIP_CUDA_TRY(cudaMalloc(&p->VhS, 2 * nVh));
+  ATRIP_CUDA_TRY(cudaMalloc(&p->VhST, 2 * nVh));
+  ATRIP_CUDA_TRY(cudaMalloc(&p->VpS, 2 * nVp));
+  ATRIP_CUDA_TRY(cudaMalloc(&p->TpS, 2 * nTp));
+  ATRIP_CUDA_TRY(cudaMalloc(&p->TpTS, 2 * nTp));
+  ATRIP_CUDA_TRY(cudaMalloc(&p->d_status, sizeof(int)));
+
+  // rows (o, r1, r2) and source strides of each slice tensor
+  SliceJob j;
+  j.S = S;
+  j.sign = 1.0;
+  // TaS[s][x][q][p][E] = T[x,E,p,q] from Ta[x][q][p][E]
+  j.src = dt.Ta; j.dst = p->TaS; j.nrows = Nv * No2; j.n1 = No; j.n2 = No;
+  j.so = No2 * Nv; j.s1 = No * Nv; j.s2 = Nv; j.sk = 1; j.K = Nv; j.Kp = (int)Ep; j.scale = sT;
+  if ((rc = run_slices(j, st))) return rc;
+  // TaST[s][x][p][q][E]: rows with q fastest
+  j.dst = p->TaST; j.s1 = Nv; j.s2 = No * Nv;
+  if ((rc = run_slices(j, st))) return rc;
+  // VhS[s][w][q][p][L] = Vh[p,q,L,w] from Vht[w][q][p][L]
+  j.src = dt.Vht; j.dst = p->VhS; j.nrows = Nv * No2; j.n1 = No; j.n2 = No;
+  j.so = No2 * No; j.s1 = No2; j.s2 = No; j.sk = 1; j.K = No; j.Kp = kHoleK; j.scale = sV;
+  if ((rc = run_slices(j, st))) return rc;
+  j.dst = p->VhST; j.s1 = No; j.s2 = No2;
+  if ((rc = run_slices(j, st))) return rc;
+  // VpS[s][y][z][r][E] = Vp[y,z,E,r] from Vpt[y][z][r][E]
+  j.src = dt.Vpt; j.dst = p->VpS; j.nrows = (int64_t)Nv * Nv * No; j.n1 = Nv; j.n2 = No;
+  j.so = (int64_t)Nv * No * Nv; j.s1 = (int64_t)No * Nv; j.s2 = Nv; j.sk = 1; j.K = Nv;
+  j.Kp = (int)Ep; j.scale = sV;
+  if ((rc = run_slices(j, st))) return rc;
+  // TpS[s][u][v][r][L] = -T[u,v,L,r] = -Tp[u][v][r][L]
+  j.src = dt.Tp; j.dst = p->TpS; j.nrows = (int64_t)Nv * Nv * No; j.n1 = Nv; j.n2 = No;
+  j.so = (int64_t)Nv * No2; j.s1 = No2; j.s2 = No; j.sk = 1; j.K = No; j.Kp = kHoleK;
+  j.scale = sT; j.sign = -1.0;
+  if ((rc = run_slices(j, st))) return rc;
+  // TpTS[s][u][v][r][L] = -T[u,v,r,L] = -Tp[u][v][L][r]
+  j.dst = p->TpTS; j.s2 = 1; j.sk = No;
+  if ((rc = run_slices(j, st))) return rc;
+  *launches += 7;
+  ATRIP_CUDA_TRY(cudaStreamSynchronize(st));
+
+  // tensor maps (all 5-D, K-dim fastest); boxes: A (64, No, jt), B (64, NP)
+  const int jt = 128 / No;
+  const int NP = No <= 16 ? 16 : No <= 32 ? 32 : No <= 48 ? 48 : 64;
+  {
+    const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt, 1, 1};
+    if ((rc = make_map(&p->maps.TaN, p->TaS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.TaT, p->TaST, d, box))) return rc;
+  }
+  {
+    const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt, 1, 1};
+    if ((rc = make_map(&p->maps.VhN, p->VhS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.VhT, p->VhST, d, box))) return rc;
+  }
+  {
+    const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)NP, 1, 1, 1};
+    if ((rc = make_map(&p->maps.Vp, p->VpS, d, box))) return rc;
+  }
+  {
+    const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)NP, 1, 1, 1};
+    if ((rc = make_map(&p->maps.TpN, p->TpS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.TpT, p->TpTS, d, box))) return rc;
+  }
+  return ATRIP_OK;
+}
+
+template <int S, int NP, bool WSMEM, bool SPLIT0>
+int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
+  using K = KernelShape<S, NP, WSMEM, SPLIT0>;
+  const int No3 = a.No * a.No * a.No;
+  const size_t wbytes = WSMEM ? 2 * sizeof(int32_t) * ((No3 + 31) & ~31) : 0;
+  const size_t avail = kSmemLimit - 1024 - kTailBytes - wbytes;
+  int nst = (int)(avail / K::kStageBytes);
+  if (nst > kMaxStages) nst = kMaxStages;
+  if (nst < 2) {
+    set_error("split form: shared memory too small for No=" + std::to_string(a.No));
+    return ATRIP_ERR_UNSUPPORTED;
+  }
+  SplitArgs args = a;
+  args.nstages = nst;
+  const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + wbytes;
+  auto kern = triples_split_kernel<S, NP, WSMEM, SPLIT0>;
+  ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  const int64_t n = a.t_end - a.t_begin;
+  const int grid = (int)(n < sm_count ? n : sm_count);
+  kern<<<grid, kThreads, smem, st>>>(p->maps, args);
+  ATRIP_CUDA_TRY(cudaGetLastError());
+  return ATRIP_OK;
+}
+
+template <int S, int NP>
+int launch_np(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
+  const bool wsmem = a.No <= 24;
+  const bool split0 = 2 * (a.Nv + a.No) > 1024;
+  if (wsmem)
+    return split0 ? launch_shape<S, NP, true, true>(p, a, sm_count, st)
+                  : launch_shape<S, NP, true, false>(p, a, sm_count, st);
+  return split0 ? launch_shape<S, NP, false, true>(p, a, sm_count, st)
+                : launch_shape<S, NP, false, false>(p, a, sm_count, st);
+}
+
+template <int S>
+int launch_s(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
+  const int No = a.No;
+  if (No <= 16) return launch_np<S, 16>(p, a, sm_count, st);
+  if (No <= 32) return launch_np<S, 32>(p, a, sm_count, st);
+  if (No <= 48) return launch_np<S, 48>(p, a, sm_count, st);
+  return launch_np<S, 64>(p, a, sm_count, st);
+}
+
+}  // namespace
 
 void split_invalidate(SplitState &s) { s.valid = false; }
-void split_free(SplitState &s) { s.valid = false; s.impl = nullptr; }
 
-int split_run(SplitState &, const DeviceTensors &, int, int, int, const uint32_t *,
-              const uint32_t *, int, int64_t, int64_t, double, bool, int, unsigned long long *,
-              double *, double *, cudaStream_t, int64_t *) {
-  set_error("split-BF16 form not built yet");
-  return ATRIP_ERR_UNSUPPORTED;
+void split_free(SplitState &s) {
+  free_impl(static_cast<SplitImpl *>(s.impl));
+  s.impl = nullptr;
+  s.valid = false;
+}
+
+int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
+              const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,
+              int64_t t_end, double tai_sign, bool use_j, int slices,
+              unsigned long long *queue, double *e, double *ect, cudaStream_t st,
+              int64_t *launches) {
+  if (slices < 2 || slices > 4) {
+    set_error("split form: slices must be 2, 3 or 4");
+    return ATRIP_ERR_ARGUMENT;
+  }
+  if (use_j) {
+    set_error("split form: the (cT) intermediates are only supported by the FP64 form");
+    return ATRIP_ERR_UNSUPPORTED;
+  }
+  if (!s.valid || s.slices != slices || !s.impl) {
+    split_free(s);
+    auto *p = new SplitImpl();
+    s.impl = p;
+    int rc = prepare(p, dt, No, Nv, slices, st, launches);
+    if (rc != ATRIP_OK) {
+      split_free(s);
+      return rc;
+    }
+    s.valid = true;
+    s.slices = slices;
+  }
+  auto *p = static_cast<SplitImpl *>(s.impl);
+  if (No > 24) {
+    const size_t need = (size_t)sm_count * 2 * No * No * No;
+    if (need > p->wglobal_floats) {
+      cudaFree(p->wglobal);
+      p->wglobal = nullptr;
+      ATRIP_CUDA_TRY(cudaMalloc(&p->wglobal, sizeof(float) * need));
+      p->wglobal_floats = need;
+    }
+  }
+  ATRIP_CUDA_TRY(cudaMemsetAsync(p->d_status, 0, sizeof(int), st));
+  SplitArgs a;
+  a.No = No;
+  a.Nv = Nv;
+  a.jt = 128 / No;
+  a.ntiles = (No + a.jt - 1) / a.jt;
+  a.kch = p->Ep / kKChunk;
+  a.epsi = dt.epsi;
+  a.epsa = dt.epsa;
+  a.tai = dt.tai;
+  a.Vhh = dt.Vhh;
+  a.tuples = tuples;
+  a.triples = triples;
+  a.n_triples = n_triples;
+  a.t_begin = t_begin;
+  a.t_end = t_end;
+  a.queue = queue;
+  a.tai_sign = tai_sign;
+  a.unit = p->unit;
+  a.e = e;
+  a.ect = ect;
+  a.status = p->d_status;
+  a.wglobal = p->wglobal;
+  int rc;
+  switch (slices) {
+    case 2: rc = launch_s<2>(p, a, sm_count, st); break;
+    case 3: rc = launch_s<3>(p, a, sm_count, st); break;
+    default: rc = launch_s<4>(p, a, sm_count, st); break;
+  }
+  if (rc != ATRIP_OK) return rc;
+  *launches += 1;
+  int status = 0;
+  ATRIP_CUDA_TRY(cudaMemcpyAsync(&status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ATRIP_CUDA_TRY(cudaStreamSynchronize(st));
+  if (status != 0) {
+    set_error("split kernel: a bounded wait gave up (code " + std::to_string(status) + ")");
+    return ATRIP_ERR_TIMEOUT;
+  }
+  return ATRIP_OK;
 }
 
 }  // namespace atrip_gb300

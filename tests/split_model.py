@@ -1,0 +1,75 @@
+"""Reference model of the split-precision arithmetic, for the tests.
+
+The split form writes each FP64 element as 2^(e-7) sum_p q_p 2^(-8p) with
+integer digits |q_p| <= 128 (one power-of-two scale per tensor: 2^eT for T,
+2^eV shared by V_pphp and V_hhhp), and keeps the digit products of level
+p + q < S.  Because the doubles contribution is bilinear in (T, V), the kept
+sum equals
+
+    W_S = sum_{p < S} doubles(T_p, V_{< S-p}),
+
+where T_p is the p-th digit component of T and V_{<m} the sum of the first
+m components of V.  This module evaluates W_S with the CPU oracle's doubles
+and energy routines (FP64 everywhere else), which is what the GPU kernel is
+expected to reproduce up to FP32 rounding of the level >= 1 partial sums.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+import oracle
+
+
+def exponent(maxabs: float) -> int:
+    return 0 if maxabs <= 0 else math.frexp(maxabs)[1]  # maxabs < 2^e
+
+
+def digit_components(x: np.ndarray, e: int, S: int):
+    """[x_0, ..., x_{S-1}]: x_p = q_p 2^(e-7-8p)."""
+    y = np.ldexp(np.asarray(x, dtype=np.float64), 7 - e)
+    out = []
+    for p in range(S):
+        q = np.rint(y)
+        assert np.max(np.abs(q)) <= 128
+        out.append(np.ldexp(q, e - 7 - 8 * p))
+        y = (y - q) * 256.0
+    return out
+
+
+def split_tuple_energies(d: dict, S: int, t0: int = 0, t1: int | None = None):
+    """Per-tuple energies of the split form's arithmetic with S slices."""
+    No, Nv = d["No"], d["Nv"]
+    eT = exponent(float(np.max(np.abs(d["Tabij"]))))
+    eV = exponent(max(float(np.max(np.abs(d["Vabci"]))), float(np.max(np.abs(d["Vijka"])))))
+    Tc = digit_components(d["Tabij"], eT, S)
+    Vpc = digit_components(d["Vabci"], eV, S)
+    Vhc = digit_components(d["Vijka"], eV, S)
+    problems = []
+    for p in range(S):
+        m = S - p
+        dd = dict(d)
+        dd["Tabij"] = np.asfortranarray(Tc[p])
+        dd["Vabci"] = np.asfortranarray(sum(Vpc[:m]))
+        dd["Vijka"] = np.asfortranarray(sum(Vhc[:m]))
+        problems.append(oracle.Problem(dd))
+    full = oracle.Problem(d)
+    lst = oracle.tuple_list(Nv)
+    t1 = len(lst) if t1 is None else t1
+    lib = oracle._load()
+    out = np.zeros(t1 - t0)
+    for n, t in enumerate(range(t0, t1)):
+        a, b, c = (int(v) for v in lst[t])
+        W = np.zeros(No ** 3)
+        for pr in problems:
+            Tp, _ = oracle.tuple_arrays(pr, a, b, c)
+            W += Tp
+        # Z = W + singles, from the full-precision problem
+        T_full, Z_full = oracle.tuple_arrays(full, a, b, c)
+        Z = W + (Z_full - T_full)
+        epsabc = d["epsa"][a] + d["epsa"][b] + d["epsa"][c]
+        eps = np.ascontiguousarray(d["epsi"], dtype=np.float64)
+        fn = lib.oracle_energy_distinct if (a != b and b != c) else lib.oracle_energy_same
+        out[n] = fn(float(epsabc), No, eps.ctypes.data, W.ctypes.data, Z.ctypes.data)
+    return out

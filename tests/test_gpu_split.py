@@ -1,0 +1,86 @@
+"""GPU parity of the split-precision form (BF16 digit slices on tcgen05).
+
+Two references:
+* the split model (tests/split_model.py): the same truncated digit products
+  evaluated in FP64 by the CPU oracle -- the kernel must reproduce it up to
+  FP32 rounding of the level >= 1 partial sums (tolerance 1e-7 relative per
+  tuple, far below the split truncation error it would expose);
+* the FP64 form: the error of the split form itself, bounded per slice count
+  (S=2: 1e-4, S=3: 1e-6, S=4: 1e-8 relative per tuple), and the benchmark's
+  |dE(T)| <= 1e-8 Eh on a power-of-two-scaled twin with |E(T)| ~ 0.1 Eh.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import split_model
+from atrip_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+BOUND = {2: 1e-4, 3: 1e-6, 4: 1e-8}
+
+
+def _ctx(d):
+    ctx = capi.Context(d["No"], d["Nv"], 0)
+    for n in ("epsi", "epsa", "Tai", "Tabij", "Vabij", "Vijka", "Vabci"):
+        ctx.upload(n, d[n])
+    return ctx
+
+
+CASES = [(6, 10, 1), (8, 40, 0), (5, 9, 3), (13, 17, 2), (24, 30, 4), (30, 14, 5), (1, 6, 7),
+         (64, 6, 8), (17, 70, 9)]
+
+
+@pytest.mark.parametrize("No,Nv,seed", CASES)
+@pytest.mark.parametrize("S", [2, 3, 4])
+def test_split_matches_model_and_fp64(No, Nv, seed, S):
+    d = synth.make_inputs(No, Nv, seed)
+    n = min(synth.n_tuples(Nv), 120)
+    model = split_model.split_tuple_energies(d, S, 0, n)
+    with _ctx(d) as ctx:
+        r64 = ctx.run(form="fp64", use_j=False, max_iterations=n - 1)
+        e64, _ = ctx.tuple_energies(0, n)
+        r = ctx.run(form="split_bf16", slices=S, use_j=False, max_iterations=n - 1)
+        assert r.form_used == capi.FORM_SPLIT_BF16 and r.slices_used == S
+        e, ect = ctx.tuple_energies(0, n)
+    assert np.array_equal(e, ect)
+    if No == 1:
+        # one occupied orbital: every tuple energy cancels to rounding noise
+        assert np.max(np.abs(e)) <= 1e-12 and np.max(np.abs(e64)) <= 1e-12
+        return
+    scale = np.max(np.abs(model))
+    assert np.max(np.abs(e - model)) <= 1e-7 * scale + 1e-14, np.max(np.abs(e - model)) / scale
+    rel = np.max(np.abs(e - e64)) / np.max(np.abs(e64))
+    assert rel <= BOUND[S], rel
+    assert abs(r.energy - r64.energy) <= BOUND[S] * abs(r64.energy)
+
+
+def test_split_scaled_twin_meets_1e8_hartree():
+    """No=8, Nv=40 with t1, t2 and all integrals scaled by 2^-k so that
+    |E(T)| ~ 0.1 Eh: |E_split - E_fp64| <= 1e-8 Eh with 3 slices."""
+    d0 = synth.make_inputs(8, 40, 0)
+    with _ctx(d0) as ctx:
+        e0 = ctx.run(form="fp64", use_j=False).energy
+    k = int(round(np.log2(abs(e0) / 0.1) / 4))
+    d = synth.make_inputs(8, 40, 0, scale=2.0 ** -k)
+    with _ctx(d) as ctx:
+        e64 = ctx.run(form="fp64", use_j=False).energy
+        e3 = ctx.run(form="split_bf16", slices=3, use_j=False).energy
+    assert 0.01 < abs(e64) < 1.0
+    assert abs(e64 * 2.0 ** (4 * k) - e0) <= 1e-12 * abs(e0)  # power-of-two scaling is exact
+    assert abs(e3 - e64) <= 1e-8, abs(e3 - e64)
+
+
+def test_split_rejects_ct_and_bad_slices():
+    d = synth.make_inputs(4, 7, 1, with_j=True)
+    with _ctx(d) as ctx:
+        ctx.upload("Jijka", d["Jijka"])
+        ctx.upload("Jabci", d["Jabci"])
+        with pytest.raises(capi.AtripError) as ei:
+            ctx.run(form="split_bf16", slices=3, use_j=True)
+        assert ei.value.status == capi.ERR_UNSUPPORTED
+        with pytest.raises(capi.AtripError) as ei:
+            ctx.run(form="split_bf16", slices=5, use_j=False)
+        assert ei.value.status == capi.ERR_ARGUMENT
+        # the FP64 form still works on the same context
+        assert np.isfinite(ctx.run(form="fp64").energy)
