@@ -53,10 +53,10 @@ namespace {
 
 using namespace sm100;
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 448;
 constexpr int kMaxStages = 6;
 constexpr int kSmemLimit = 232448;  // opt-in dynamic shared memory per block
-constexpr int kTailBytes = 256 + 3 * 64 * 8 + 16 * 8;  // barriers, t1 rows, reduction
+constexpr int kTailBytes = 384 + 3 * 64 * 8 + 16 * 8;  // + 3 No^2 doubles (singles)
 constexpr int kKChunk = 64;              // BF16 elements per 128-byte row
 constexpr int kATileBytes = 128 * 128;   // 128 rows x 128 B
 constexpr int kHoleK = 64;               // hole K (L) padded to one chunk
@@ -83,7 +83,7 @@ struct SplitArgs {
   double tai_sign, unit;
   double *e, *ect;
   int *status;
-  float *wglobal;  // per-CTA W (int32 + float) when it does not fit in smem
+  float *wglobal;  // two W buffers per CTA (one 8-byte cell per element)
 };
 
 // ------------------------------------------------------------------ prep
@@ -175,7 +175,7 @@ __device__ __forceinline__ Part part_of(const SplitMaps &m, int g, int pt, int a
   return p;
 }
 
-template <int S, int NP, bool WSMEM, bool SPLIT0>
+template <int S, int NP, bool SPLIT0>
 struct KernelShape {
   static constexpr int kNacc = S + (SPLIT0 ? 1 : 0);
   static constexpr int kBufCols = kNacc * NP;
@@ -187,37 +187,54 @@ struct KernelShape {
   static constexpr int kStageBytes = kATileBytes + S * kBTile;
 };
 
-template <int S, int NP, bool WSMEM, bool SPLIT0>
+// Tuple hand-off ring: the producer owns the work queue and publishes each
+// tuple to the MMA issuer, the epilogue warps and the energy warps.
+constexpr int kTupleSlots = 4;
+constexpr int kEnergyWarps = 8;  // warps 2, 3 and 8 .. 13
+constexpr int kEnergyThreads = kEnergyWarps * 32;
+
+struct TupleSlot {
+  int64_t t;  // list position, -1 = no more work
+  int a, b, c;
+};
+
+__device__ __forceinline__ int energy_rank(int warp, int lane) {
+  return ((warp < 4 ? warp - 2 : warp - 6) << 5) | lane;
+}
+
+// W cells live in global memory (L2-resident, two buffers per CTA): one
+// 8-byte cell per element, {int32 level-0 sum, float rest} while the groups
+// accumulate, then the FP64 value written over the same 8 bytes.  The
+// epilogue warps fill buffer k % 2 for tuple k while the energy warps read
+// buffer (k-1) % 2, so the tensor-core work of one tuple overlaps the FP64
+// energy evaluation of the previous one.
+template <int S, int NP, bool SPLIT0>
 __global__ void __launch_bounds__(kThreads, 1)
     triples_split_kernel(const __grid_constant__ SplitMaps maps, const SplitArgs g) {
-  using K = KernelShape<S, NP, WSMEM, SPLIT0>;
+  using K = KernelShape<S, NP, SPLIT0>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char *ring = smem;
-  const int No = g.No, No3 = No * No * No;
-  int32_t *WI;
-  float *WF;
+  const int No = g.No, No2 = No * No, No3 = No2 * No;
   const int kStages = g.nstages;
   unsigned char *tail = ring + kStages * K::kStageBytes;
-  if (WSMEM) {
-    WI = reinterpret_cast<int32_t *>(tail);
-    WF = reinterpret_cast<float *>(tail + sizeof(int32_t) * No3);
-    tail += 2 * sizeof(int32_t) * ((No3 + 31) & ~31);
-  } else {
-    WI = reinterpret_cast<int32_t *>(g.wglobal + (size_t)blockIdx.x * 2 * No3);
-    WF = g.wglobal + (size_t)blockIdx.x * 2 * No3 + No3;
-  }
+  double *Wbase = reinterpret_cast<double *>(g.wglobal) + (size_t)blockIdx.x * 2 * No3;
   uint64_t *full = reinterpret_cast<uint64_t *>(tail);
-  uint64_t *empty = full + kStages;
-  uint64_t *accf = empty + kStages;
+  uint64_t *empty = full + kMaxStages;
+  uint64_t *accf = empty + kMaxStages;
   uint64_t *acce = accf + 2;
-  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(acce + 2);
-  int *slot_holder = reinterpret_cast<int *>(tmem_holder + 1);
-  double *ta = reinterpret_cast<double *>(tail + 256);
+  uint64_t *tfull = acce + 2;
+  uint64_t *tempty = tfull + kTupleSlots;
+  uint64_t *wfull = tempty + kTupleSlots;
+  uint64_t *wfree = wfull + 2;
+  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(wfree + 2);
+  TupleSlot *tslot = reinterpret_cast<TupleSlot *>(tail + 256);
+  double *ta = reinterpret_cast<double *>(tail + 384);
   double *tb = ta + 64;
   double *tc = tb + 64;
-  double *red = tc + 64;  // [8][2]
+  double *red = tc + 64;   // [kEnergyWarps]
+  double *Vsm = red + 16;  // 3 No x No blocks for the singles
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -228,6 +245,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf[b], 1);
       mbar_init(&acce[b], 128);
+      mbar_init(&wfull[b], 1);
+      mbar_init(&wfree[b], 1);
+    }
+    for (int s = 0; s < kTupleSlots; ++s) {
+      mbar_init(&tfull[s], 1);
+      mbar_init(&tempty[s], 3);
     }
     fence_mbar_init();
     prefetch_tensormap(&maps.TaN);
@@ -249,47 +272,39 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
-
-  const uint32_t idesc = idesc_bf16_f32(128, NP);
   const int jt = g.jt, ntiles = g.ntiles, kch = g.kch;
   const int a_bytes = 128 * No * jt;  // full A box, out-of-range rows included
-  // role-local pipeline counters (persist across tuples)
-  uint32_t unit_count = 0, item_count = 0;
-  bool alive = true;
 
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const unsigned long long q = atomicAdd(g.queue, 1ull);
-      const bool stop = q >= (unsigned long long)(g.t_end - g.t_begin) ||
-                        *reinterpret_cast<volatile int *>(g.status) != 0;
-      *slot_holder = stop ? -1 : (int)q;
-    }
-    __syncthreads();
-    const int slot = *slot_holder;
-    if (slot < 0) break;
-    const int64_t t = g.t_begin + slot;
-    const uint32_t pk = g.tuples[t];
-    const int a = pk & 0x3ff, b = (pk >> 10) & 0x3ff, c = (pk >> 20) & 0x3ff;
-    for (int i = threadIdx.x; i < No3; i += kThreads) {
-      WI[i] = 0;
-      WF[i] = 0.f;
-    }
-    if (threadIdx.x < No) {
-      const int i = threadIdx.x;
-      ta[i] = g.tai_sign * g.tai[a + i * g.Nv];
-      tb[i] = g.tai_sign * g.tai[b + i * g.Nv];
-      tc[i] = g.tai_sign * g.tai[c + i * g.Nv];
-    }
-    __syncthreads();
-
-    if (warp == 0) {
-      // ---------------------------------------------------- TMA producer
-      if (lane == 0 && alive) {
+  if (warp == 0) {
+    // ------------------------------------------------------ TMA producer
+    if (lane == 0) {
+      uint32_t unit_count = 0;
+      bool alive = true;
+      for (uint32_t k = 0;; ++k) {
+        const int ts = k % kTupleSlots;
+        const uint32_t tuse = k / kTupleSlots;
+        if (tuse > 0 && !mbar_wait(&tempty[ts], (tuse - 1) & 1, g.status, kErrTimeoutEmpty))
+          alive = false;
+        const unsigned long long q = alive ? atomicAdd(g.queue, 1ull) : ~0ull;
+        const bool stop = !alive || q >= (unsigned long long)(g.t_end - g.t_begin) ||
+                          *reinterpret_cast<volatile int *>(g.status) != 0;
+        TupleSlot s;
+        s.t = stop ? -1 : g.t_begin + (int64_t)q;
+        s.a = s.b = s.c = 0;
+        if (!stop) {
+          const uint32_t pk = g.tuples[s.t];
+          s.a = pk & 0x3ff;
+          s.b = (pk >> 10) & 0x3ff;
+          s.c = (pk >> 20) & 0x3ff;
+        }
+        tslot[ts] = s;
+        mbar_arrive(&tfull[ts]);  // release: the slot is visible to the waiters
+        if (stop) break;
         for (int grp = 0; grp < 3 && alive; ++grp)
           for (int mt = 0; mt < ntiles && alive; ++mt) {
             const int j0 = mt * jt;
             for (int pt = 0; pt < 4 && alive; ++pt) {
-              const Part p = part_of(maps, grp, pt, a, b, c);
+              const Part p = part_of(maps, grp, pt, s.a, s.b, s.c);
               const int nch = p.particle ? kch : 1;
               for (int ch = 0; ch < nch && alive; ++ch)
                 for (int sa = 0; sa < S; ++sa) {
@@ -311,9 +326,19 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
       }
-    } else if (warp == 1) {
-      // ------------------------------------------------------ MMA issuer
-      if (lane == 0 && alive) {
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // -------------------------------------------------------- MMA issuer
+    if (lane == 0) {
+      uint32_t unit_count = 0, item_count = 0;
+      bool alive = true;
+      for (uint32_t k = 0;; ++k) {
+        const int ts = k % kTupleSlots;
+        if (!mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull)) break;
+        const int64_t t = tslot[ts].t;
+        mbar_arrive(&tempty[ts]);
+        if (t < 0) break;
         for (int it = 0; it < 3 * ntiles && alive; ++it) {
           const int buf = item_count % K::kNbuf;
           const uint32_t use = item_count / K::kNbuf;
@@ -322,9 +347,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           tc_fence_after();
-          bool fresh[K::kNacc];
-#pragma unroll
-          for (int q = 0; q < K::kNacc; ++q) fresh[q] = true;
+          bool fresh_main = true, fresh_tr0 = true;
           const uint32_t dbase = tmem + buf * K::kBufCols;
           for (int pt = 0; pt < 4 && alive; ++pt) {
             const int nch = (pt & 1) == 0 ? kch : 1;
@@ -339,18 +362,31 @@ __global__ void __launch_bounds__(kThreads, 1)
                 tc_fence_after();
                 const uint32_t sbase = smem_u32(ring + st * K::kStageBytes);
                 const uint64_t adesc = sdesc_sw128(sbase);
+                const uint64_t bdesc = sdesc_sw128(sbase + kATileBytes);
+                // A slice sa against B slices 0 .. S-1-sa in one MMA: the
+                // result columns are the level accumulators sa .. S-1, which
+                // sit side by side in TMEM.
+                if (SPLIT0 && pt >= 2 && sa == 0) {
+                  // level 0 of the transposed half has its own accumulator
 #pragma unroll
-                for (int sb = 0; sb < S; ++sb) {
-                  if (sb < S - sa) {
-                    const int level = sa + sb;
-                    const int acc = (SPLIT0 && level == 0 && pt >= 2) ? S : level;
-                    const uint64_t bdesc = sdesc_sw128(sbase + kATileBytes + sb * K::kBTile);
+                  for (int kk = 0; kk < kKChunk / 16; ++kk)
+                    mma_bf16(dbase + S * NP, adesc + 2 * kk, bdesc + 2 * kk,
+                             idesc_bf16_f32(128, NP), (fresh_tr0 && kk == 0) ? 0u : 1u);
+                  fresh_tr0 = false;
+                  if (S > 1) {
+                    const uint64_t bdesc1 = sdesc_sw128(sbase + kATileBytes + K::kBTile);
 #pragma unroll
                     for (int kk = 0; kk < kKChunk / 16; ++kk)
-                      mma_bf16(dbase + acc * NP, adesc + 2 * kk, bdesc + 2 * kk, idesc,
-                               (fresh[acc] && kk == 0) ? 0u : 1u);
-                    fresh[acc] = false;
+                      mma_bf16(dbase + NP, adesc + 2 * kk, bdesc1 + 2 * kk,
+                               idesc_bf16_f32(128, (S - 1) * NP), 1u);
                   }
+                } else {
+                  const uint32_t id = idesc_bf16_f32(128, (S - sa) * NP);
+#pragma unroll
+                  for (int kk = 0; kk < kKChunk / 16; ++kk)
+                    mma_bf16(dbase + sa * NP, adesc + 2 * kk, bdesc + 2 * kk, id,
+                             (fresh_main && kk == 0) ? 0u : 1u);
+                  fresh_main = false;
                 }
                 mma_commit(&empty[st]);
                 ++unit_count;
@@ -359,28 +395,44 @@ __global__ void __launch_bounds__(kThreads, 1)
           mma_commit(&accf[buf]);
           ++item_count;
         }
+        if (!alive) break;
       }
-    } else if (warp >= 4) {
-      // -------------------------------------------------------- epilogue
-      const int quarter = warp - 4;
-      const int l = quarter * 32 + lane;
+    }
+    __syncwarp();
+  } else if (warp >= 4 && warp < 8) {
+    // ------------------------------------------------ epilogue (4 warps)
+    // warp % 4 selects the 32-lane TMEM quarter this warp may read
+    const int quarter = warp - 4;
+    const int l = quarter * 32 + lane;
+    uint32_t item_count = 0;
+    bool alive = true;
+    for (uint32_t k = 0;; ++k) {
+      const int ts = k % kTupleSlots;
+      bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull);
+      const int64_t t = tslot[ts].t;
+      named_bar_sync(1, 128);
+      if (threadIdx.x == 128) mbar_arrive(&tempty[ts]);
+      if (!ok || t < 0) break;
+      const int wb = k & 1;
+      const uint32_t wuse = k >> 1;
+      ok = wuse == 0 || mbar_wait(&wfree[wb], (wuse - 1) & 1, g.status, kErrTimeoutEmpty);
+      int2 *Wc = reinterpret_cast<int2 *>(Wbase + (size_t)wb * No3);
       for (int it = 0; it < 3 * ntiles; ++it) {
         const int grp = it / ntiles, mt = it % ntiles;
         const int buf = item_count % K::kNbuf;
         const uint32_t use = item_count / K::kNbuf;
-        bool ok = alive && mbar_wait(&accf[buf], use & 1, g.status, kErrTimeoutAccFull);
-        // the whole warp takes part in tcgen05.ld, so agree on ok; a failed
-        // wait skips the loads but still meets the named barrier below, so
-        // the four epilogue warps always execute the same barriers
-        ok = __all_sync(0xffffffffu, ok);
-        if (!ok) alive = false;
+        bool okw = ok && alive && mbar_wait(&accf[buf], use & 1, g.status, kErrTimeoutAccFull);
+        // tcgen05.ld is warp-collective: agree; a failed wait skips the
+        // loads but meets the same barriers as the other epilogue warps
+        okw = __all_sync(0xffffffffu, okw);
+        if (!okw) alive = false;
         tc_fence_after();
         const int j0 = mt * jt;
         const int rows = No * min(jt, No - j0);
         const bool valid = l < rows;
         const int f = l % No, sl = j0 + l / No;
         const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + buf * K::kBufCols;
-        for (int c0 = 0; c0 < NP && ok; c0 += 16) {
+        for (int c0 = 0; c0 < NP && okw; c0 += 16) {
           float v[K::kNacc][16];
 #pragma unroll
           for (int q = 0; q < K::kNacc; ++q) tmem_ld16(tbase + q * NP + c0, v[q]);
@@ -390,94 +442,133 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int cc = 0; cc < 16; ++cc) {
               const int col = c0 + cc;
               if (col < No) {
-                int i, jj, k;
-                if (grp == 0) { i = f; jj = sl; k = col; }
-                else if (grp == 1) { i = f; k = sl; jj = col; }
-                else { jj = f; k = sl; i = col; }
-                const int idx = i + No * (jj + No * k);
+                int i, jj, kx;
+                if (grp == 0) { i = f; jj = sl; kx = col; }
+                else if (grp == 1) { i = f; kx = sl; jj = col; }
+                else { jj = f; kx = sl; i = col; }
+                const int idx = i + No * (jj + No * kx);
                 int lev0 = __float2int_rn(v[0][cc]);
                 if (SPLIT0) lev0 += __float2int_rn(v[S][cc]);
                 float rest = 0.f;
 #pragma unroll
                 for (int q = S - 1; q >= 1; --q) rest = rest * (1.f / 256.f) + v[q][cc];
                 rest *= (1.f / 256.f);
-                WI[idx] += lev0;
-                WF[idx] += rest;
+                int2 cell = Wc[idx];
+                cell.x += lev0;
+                cell.y = __float_as_int(__int_as_float(cell.y) + rest);
+                Wc[idx] = cell;
               }
             }
           }
         }
         tc_fence_before();
         mbar_arrive(&acce[buf]);
-        named_bar_sync(1, 128);
+        named_bar_sync(1, 128);  // orders the scatters of consecutive items
         ++item_count;
       }
+      // W of tuple k complete: hand it to the energy warps
+      __threadfence_block();
+      named_bar_sync(1, 128);
+      if (threadIdx.x == 128) mbar_arrive(&wfull[wb]);
     }
     __syncwarp();
-    __syncthreads();
-    {
-      int bad = *reinterpret_cast<volatile int *>(g.status) != 0;
-      if (bad) alive = false;
-    }
-
-    // ---------------------------------------------------------- energy
-    int cls = 0;  // src/atrip/Atrip.cxx:640-642
-    if (a == b) cls++;
-    if (b == c) cls--;
-    const bool distinct = cls == 0;
-    const double epsabc = g.epsa[a] + g.epsa[b] + g.epsa[c];
-    const int64_t Nv = g.Nv, No2 = (int64_t)No * No;
-    const double *Vbc = g.Vhh + ((int64_t)b * Nv + c) * No2;
-    const double *Vac = g.Vhh + ((int64_t)a * Nv + c) * No2;
-    const double *Vab = g.Vhh + ((int64_t)a * Nv + b) * No2;
-    const double unit = g.unit;
-    auto W = [&](int i, int j, int k) {
-      const int idx = i + No * (j + No * k);
-      return unit * ((double)WI[idx] + (double)WF[idx]);
-    };
-    auto Zv = [&](int i, int j, int k) {
-      double z = W(i, j, k);
-      z += ta[i] * Vbc[j + k * No];
-      z += tb[j] * Vac[i + k * No];
-      z += tc[k] * Vab[i + j * No];
-      return z;
-    };
-    double sum = 0.0;
-    for (int n = threadIdx.x; n < g.n_triples; n += kThreads) {
-      const uint32_t tp = g.triples[n];
-      const int i = tp & 0xff, j = (tp >> 8) & 0xff, k = (tp >> 16) & 0xff;
-      const double facjk = j == k ? 0.5 : 1.0, facij = i == j ? 0.5 : 1.0;
-      const double denominator = epsabc - ((g.epsi[i] + g.epsi[j]) + g.epsi[k]);
-      double value;
-      if (distinct) {
-        const double U = Zv(i, j, k), V = Zv(i, k, j), Wv = Zv(j, i, k), X = Zv(j, k, i),
-                     Y = Zv(k, i, j), Z = Zv(k, j, i);
-        const double A = W(i, j, k), B = W(i, k, j), C = W(j, i, k), D = W(j, k, i),
-                     E = W(k, i, j), F = W(k, j, i);
-        const double UXY = U + (X + Y), VWZ = V + (Wv + Z), ADE = A + (D + E), BCF = B + (C + F);
-        const double first = A * U + (B * V + (C * Wv + (D * X + (E * Y + F * Z))));
-        value = 3.0 * first + ((UXY - 2.0 * VWZ) * ADE + (VWZ - 2.0 * UXY) * BCF);
-      } else {
-        const double U = Zv(i, j, k), V = Zv(j, k, i), Wv = Zv(k, i, j);
-        const double A = W(i, j, k), B = W(j, k, i), C = W(k, i, j);
-        value = 3.0 * ((A * U + B * V) + C * Wv) - (A + (B + C)) * (U + (V + Wv));
+  } else if (warp < 14) {
+    // ------------------------------------------------ energy (8 warps)
+    const int er = energy_rank(warp, lane);
+    const int64_t Nv = g.Nv;
+    for (uint32_t k = 0;; ++k) {
+      const int ts = k % kTupleSlots;
+      bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull);
+      const TupleSlot s = tslot[ts];
+      named_bar_sync(2, kEnergyThreads);
+      if (er == 0) mbar_arrive(&tempty[ts]);
+      if (!ok || s.t < 0) break;
+      const int a = s.a, b = s.b, c = s.c;
+      if (er < No) {
+        ta[er] = g.tai_sign * g.tai[a + er * Nv];
+        tb[er] = g.tai_sign * g.tai[b + er * Nv];
+        tc[er] = g.tai_sign * g.tai[c + er * Nv];
       }
-      sum += (2.0 * value / denominator) * (facjk * facij);
-    }
+      {
+        const double *Vbc = g.Vhh + ((int64_t)b * Nv + c) * No2;
+        const double *Vac = g.Vhh + ((int64_t)a * Nv + c) * No2;
+        const double *Vab = g.Vhh + ((int64_t)a * Nv + b) * No2;
+        for (int i = er; i < No2; i += kEnergyThreads) {
+          Vsm[i] = Vbc[i];
+          Vsm[No2 + i] = Vac[i];
+          Vsm[2 * No2 + i] = Vab[i];
+        }
+      }
+      const int wb = k & 1;
+      ok = mbar_wait(&wfull[wb], (k >> 1) & 1, g.status, kErrTimeoutAccFull);
+      double *Wd = Wbase + (size_t)wb * No3;
+      const int2 *Wc = reinterpret_cast<const int2 *>(Wd);
+      // W = unit * (level-0 integer + rest), converted in place to FP64
+      const double unit = g.unit;
+      for (int i = er; i < No3; i += kEnergyThreads) {
+        const int2 cell = Wc[i];
+        Wd[i] = unit * ((double)cell.x + (double)__int_as_float(cell.y));
+      }
+      named_bar_sync(2, kEnergyThreads);
+
+      int cls = 0;  // src/atrip/Atrip.cxx:640-642
+      if (a == b) cls++;
+      if (b == c) cls--;
+      const bool distinct = cls == 0;
+      const double epsabc = g.epsa[a] + g.epsa[b] + g.epsa[c];
+      const double *Vbc = Vsm, *Vac = Vsm + No2, *Vab = Vsm + 2 * No2;
+      auto W = [&](int i, int j, int kx) { return Wd[i + No * (j + No * kx)]; };
+      auto Zv = [&](int i, int j, int kx) {
+        double z = W(i, j, kx);
+        z += ta[i] * Vbc[j + kx * No];
+        z += tb[j] * Vac[i + kx * No];
+        z += tc[kx] * Vab[i + j * No];
+        return z;
+      };
+      double sum = 0.0;
+      for (int n = er; n < g.n_triples && ok; n += kEnergyThreads) {
+        const uint32_t tp = g.triples[n];
+        const int i = tp & 0xff, j = (tp >> 8) & 0xff, kx = (tp >> 16) & 0xff;
+        const double facjk = j == kx ? 0.5 : 1.0, facij = i == j ? 0.5 : 1.0;
+        const double denominator = epsabc - ((g.epsi[i] + g.epsi[j]) + g.epsi[kx]);
+        double value;
+        if (distinct) {
+          const double U = Zv(i, j, kx), V = Zv(i, kx, j), Wv = Zv(j, i, kx), X = Zv(j, kx, i),
+                       Y = Zv(kx, i, j), Z = Zv(kx, j, i);
+          const double A = W(i, j, kx), B = W(i, kx, j), C = W(j, i, kx), D = W(j, kx, i),
+                       E = W(kx, i, j), F = W(kx, j, i);
+          const double UXY = U + (X + Y), VWZ = V + (Wv + Z), ADE = A + (D + E),
+                       BCF = B + (C + F);
+          const double first = A * U + (B * V + (C * Wv + (D * X + (E * Y + F * Z))));
+          value = 3.0 * first + ((UXY - 2.0 * VWZ) * ADE + (VWZ - 2.0 * UXY) * BCF);
+        } else {
+          const double U = Zv(i, j, kx), V = Zv(j, kx, i), Wv = Zv(kx, i, j);
+          const double A = W(i, j, kx), B = W(j, kx, i), C = W(kx, i, j);
+          value = 3.0 * ((A * U + B * V) + C * Wv) - (A + (B + C)) * (U + (V + Wv));
+        }
+        sum += (2.0 * value / denominator) * (facjk * facij);
+      }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    if (lane == 0) red[warp] = sum;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double e = 0.0;
-      for (int w = 0; w < kThreads / 32; ++w) e += red[w];
-      g.e[t] = e;
-      g.ect[t] = e;
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0) red[er >> 5] = sum;
+      named_bar_sync(2, kEnergyThreads);
+      if (er == 0) {
+        double e = 0.0;
+        for (int w = 0; w < kEnergyWarps; ++w) e += red[w];
+        g.e[s.t] = e;
+        g.ect[s.t] = e;
+      }
+      // zero the buffer for the tuple after next, then release it
+      for (int i = er; i < No3; i += kEnergyThreads) Wd[i] = 0.0;
+      __threadfence_block();
+      named_bar_sync(2, kEnergyThreads);
+      if (er == 0) mbar_arrive(&wfree[wb]);
     }
-    __syncthreads();
+    __syncwarp();
   }
 
-  // Leave only after every tcgen05 op of this CTA has completed.
+  // Leave only after every tcgen05 op of this CTA has completed: the
+  // epilogue has drained every accumulator it was handed.
   __syncthreads();
   tc_fence_after();
   if (warp == 1) tmem_dealloc(tmem, K::kAllocCols);
@@ -668,12 +759,11 @@ int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, cudaSt
   return ATRIP_OK;
 }
 
-template <int S, int NP, bool WSMEM, bool SPLIT0>
+template <int S, int NP, bool SPLIT0>
 int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
-  using K = KernelShape<S, NP, WSMEM, SPLIT0>;
-  const int No3 = a.No * a.No * a.No;
-  const size_t wbytes = WSMEM ? 2 * sizeof(int32_t) * ((No3 + 31) & ~31) : 0;
-  const size_t avail = kSmemLimit - 1024 - kTailBytes - wbytes;
+  using K = KernelShape<S, NP, SPLIT0>;
+  const size_t vbytes = sizeof(double) * 3 * (size_t)a.No * a.No;
+  const size_t avail = kSmemLimit - 1024 - kTailBytes - vbytes;
   int nst = (int)(avail / K::kStageBytes);
   if (nst > kMaxStages) nst = kMaxStages;
   if (nst < 2) {
@@ -682,8 +772,8 @@ int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st
   }
   SplitArgs args = a;
   args.nstages = nst;
-  const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + wbytes;
-  auto kern = triples_split_kernel<S, NP, WSMEM, SPLIT0>;
+  const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
+  auto kern = triples_split_kernel<S, NP, SPLIT0>;
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   const int64_t n = a.t_end - a.t_begin;
@@ -695,13 +785,9 @@ int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st
 
 template <int S, int NP>
 int launch_np(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
-  const bool wsmem = a.No <= 24;
   const bool split0 = 2 * (a.Nv + a.No) > 1024;
-  if (wsmem)
-    return split0 ? launch_shape<S, NP, true, true>(p, a, sm_count, st)
-                  : launch_shape<S, NP, true, false>(p, a, sm_count, st);
-  return split0 ? launch_shape<S, NP, false, true>(p, a, sm_count, st)
-                : launch_shape<S, NP, false, false>(p, a, sm_count, st);
+  return split0 ? launch_shape<S, NP, true>(p, a, sm_count, st)
+                : launch_shape<S, NP, false>(p, a, sm_count, st);
 }
 
 template <int S>
@@ -749,14 +835,16 @@ int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_cou
     s.slices = slices;
   }
   auto *p = static_cast<SplitImpl *>(s.impl);
-  if (No > 24) {
-    const size_t need = (size_t)sm_count * 2 * No * No * No;
+  {
+    // two W buffers (one double per element) per CTA, zeroed before launch
+    const size_t need = (size_t)sm_count * 2 * 2 * No * No * No;  // in floats
     if (need > p->wglobal_floats) {
       cudaFree(p->wglobal);
       p->wglobal = nullptr;
       ATRIP_CUDA_TRY(cudaMalloc(&p->wglobal, sizeof(float) * need));
       p->wglobal_floats = need;
     }
+    ATRIP_CUDA_TRY(cudaMemsetAsync(p->wglobal, 0, sizeof(float) * need, st));
   }
   ATRIP_CUDA_TRY(cudaMemsetAsync(p->d_status, 0, sizeof(int), st));
   SplitArgs a;
