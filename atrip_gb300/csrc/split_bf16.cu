@@ -56,7 +56,7 @@ using namespace sm100;
 constexpr int kThreads = 448;
 constexpr int kMaxStages = 6;
 constexpr int kSmemLimit = 232448;  // opt-in dynamic shared memory per block
-constexpr int kTailBytes = 384 + 3 * 64 * 8 + 16 * 8;  // + 3 No^2 doubles (singles)
+constexpr int kTailBytes = 384 + 3 * 64 * 8 + 16 * 8 + 64 * 8;  // + singles blocks (+ W copy)
 constexpr int kKChunk = 64;              // BF16 elements per 128-byte row
 constexpr int kATileBytes = 128 * 128;   // 128 rows x 128 B
 constexpr int kHoleK = 64;               // hole K (L) padded to one chunk
@@ -208,7 +208,7 @@ __device__ __forceinline__ int energy_rank(int warp, int lane) {
 // epilogue warps fill buffer k % 2 for tuple k while the energy warps read
 // buffer (k-1) % 2, so the tensor-core work of one tuple overlaps the FP64
 // energy evaluation of the previous one.
-template <int S, int NP, bool SPLIT0>
+template <int S, int NP, bool SPLIT0, bool WSMEM>
 __global__ void __launch_bounds__(kThreads, 1)
     triples_split_kernel(const __grid_constant__ SplitMaps maps, const SplitArgs g) {
   using K = KernelShape<S, NP, SPLIT0>;
@@ -233,8 +233,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   double *ta = reinterpret_cast<double *>(tail + 384);
   double *tb = ta + 64;
   double *tc = tb + 64;
-  double *red = tc + 64;   // [kEnergyWarps]
-  double *Vsm = red + 16;  // 3 No x No blocks for the singles
+  double *red = tc + 64;        // [kEnergyWarps]
+  double *esm = red + 16;       // eps_i
+  double *Vsm = esm + 64;       // 3 No x No blocks for the singles
+  double *Wsm = Vsm + 3 * No2;  // FP64 copy of W for the energy loop (WSMEM)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -438,27 +440,41 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int q = 0; q < K::kNacc; ++q) tmem_ld16(tbase + q * NP + c0, v[q]);
           tmem_wait_ld();
           if (valid) {
+            // level-0 integer and weighted rest of the 16 columns
+            int lev0[16];
+            float rest[16];
+#pragma unroll
+            for (int cc = 0; cc < 16; ++cc) {
+              lev0[cc] = __float2int_rn(v[0][cc]);
+              if (SPLIT0) lev0[cc] += __float2int_rn(v[S][cc]);
+              float r = 0.f;
+#pragma unroll
+              for (int q = S - 1; q >= 1; --q) r = r * (1.f / 256.f) + v[q][cc];
+              rest[cc] = r * (1.f / 256.f);
+            }
+            // the 16 cells are distinct elements of W: issue every load
+            // before any store so the round trips to L2 overlap
+            int idx[16];
+            int2 cell[16];
 #pragma unroll
             for (int cc = 0; cc < 16; ++cc) {
               const int col = c0 + cc;
-              if (col < No) {
-                int i, jj, kx;
-                if (grp == 0) { i = f; jj = sl; kx = col; }
-                else if (grp == 1) { i = f; kx = sl; jj = col; }
-                else { jj = f; kx = sl; i = col; }
-                const int idx = i + No * (jj + No * kx);
-                int lev0 = __float2int_rn(v[0][cc]);
-                if (SPLIT0) lev0 += __float2int_rn(v[S][cc]);
-                float rest = 0.f;
-#pragma unroll
-                for (int q = S - 1; q >= 1; --q) rest = rest * (1.f / 256.f) + v[q][cc];
-                rest *= (1.f / 256.f);
-                int2 cell = Wc[idx];
-                cell.x += lev0;
-                cell.y = __float_as_int(__int_as_float(cell.y) + rest);
-                Wc[idx] = cell;
-              }
+              int i, jj, kx;
+              if (grp == 0) { i = f; jj = sl; kx = col; }
+              else if (grp == 1) { i = f; kx = sl; jj = col; }
+              else { jj = f; kx = sl; i = col; }
+              idx[cc] = col < No ? i + No * (jj + No * kx) : -1;
             }
+#pragma unroll
+            for (int cc = 0; cc < 16; ++cc)
+              if (idx[cc] >= 0) cell[cc] = __ldcg(&Wc[idx[cc]]);
+#pragma unroll
+            for (int cc = 0; cc < 16; ++cc)
+              if (idx[cc] >= 0) {
+                cell[cc].x += lev0[cc];
+                cell[cc].y = __float_as_int(__int_as_float(cell[cc].y) + rest[cc]);
+                __stcg(&Wc[idx[cc]], cell[cc]);
+              }
           }
         }
         tc_fence_before();
@@ -499,17 +515,24 @@ __global__ void __launch_bounds__(kThreads, 1)
           Vsm[2 * No2 + i] = Vab[i];
         }
       }
+      if (er < No) esm[er] = g.epsi[er];
       const int wb = k & 1;
       ok = mbar_wait(&wfull[wb], (k >> 1) & 1, g.status, kErrTimeoutAccFull);
-      double *Wd = Wbase + (size_t)wb * No3;
-      const int2 *Wc = reinterpret_cast<const int2 *>(Wd);
-      // W = unit * (level-0 integer + rest), converted in place to FP64
+      double *Wg = Wbase + (size_t)wb * No3;
+      int2 *Wc = reinterpret_cast<int2 *>(Wg);
+      // W = unit * (level-0 integer + rest) in FP64: copied into shared
+      // memory (the buffer is zeroed and handed back to the epilogue at
+      // once), or, when it does not fit, converted in place
       const double unit = g.unit;
+      double *Wd = WSMEM ? Wsm : Wg;
       for (int i = er; i < No3; i += kEnergyThreads) {
         const int2 cell = Wc[i];
         Wd[i] = unit * ((double)cell.x + (double)__int_as_float(cell.y));
+        if (WSMEM) Wc[i] = make_int2(0, 0);
       }
+      __threadfence_block();
       named_bar_sync(2, kEnergyThreads);
+      if (WSMEM && er == 0) mbar_arrive(&wfree[wb]);
 
       int cls = 0;  // src/atrip/Atrip.cxx:640-642
       if (a == b) cls++;
@@ -530,7 +553,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t tp = g.triples[n];
         const int i = tp & 0xff, j = (tp >> 8) & 0xff, kx = (tp >> 16) & 0xff;
         const double facjk = j == kx ? 0.5 : 1.0, facij = i == j ? 0.5 : 1.0;
-        const double denominator = epsabc - ((g.epsi[i] + g.epsi[j]) + g.epsi[kx]);
+        const double denominator = epsabc - ((esm[i] + esm[j]) + esm[kx]);
         double value;
         if (distinct) {
           const double U = Zv(i, j, kx), V = Zv(i, kx, j), Wv = Zv(j, i, kx), X = Zv(j, kx, i),
@@ -558,11 +581,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         g.e[s.t] = e;
         g.ect[s.t] = e;
       }
-      // zero the buffer for the tuple after next, then release it
-      for (int i = er; i < No3; i += kEnergyThreads) Wd[i] = 0.0;
-      __threadfence_block();
-      named_bar_sync(2, kEnergyThreads);
-      if (er == 0) mbar_arrive(&wfree[wb]);
+      if (!WSMEM) {
+        // zero the buffer for the tuple after next, then release it
+        for (int i = er; i < No3; i += kEnergyThreads) Wd[i] = 0.0;
+        __threadfence_block();
+      }
+      named_bar_sync(2, kEnergyThreads);  // Wsm / red reused by the next tuple
+      if (!WSMEM && er == 0) mbar_arrive(&wfree[wb]);
     }
     __syncwarp();
   }
@@ -759,10 +784,11 @@ int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, cudaSt
   return ATRIP_OK;
 }
 
-template <int S, int NP, bool SPLIT0>
+template <int S, int NP, bool SPLIT0, bool WSMEM>
 int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   using K = KernelShape<S, NP, SPLIT0>;
-  const size_t vbytes = sizeof(double) * 3 * (size_t)a.No * a.No;
+  const size_t No3 = (size_t)a.No * a.No * a.No;
+  const size_t vbytes = sizeof(double) * (3 * (size_t)a.No * a.No + (WSMEM ? No3 : 0));
   const size_t avail = kSmemLimit - 1024 - kTailBytes - vbytes;
   int nst = (int)(avail / K::kStageBytes);
   if (nst > kMaxStages) nst = kMaxStages;
@@ -773,7 +799,7 @@ int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st
   SplitArgs args = a;
   args.nstages = nst;
   const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
-  auto kern = triples_split_kernel<S, NP, SPLIT0>;
+  auto kern = triples_split_kernel<S, NP, SPLIT0, WSMEM>;
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   const int64_t n = a.t_end - a.t_begin;
@@ -786,8 +812,13 @@ int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st
 template <int S, int NP>
 int launch_np(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   const bool split0 = 2 * (a.Nv + a.No) > 1024;
-  return split0 ? launch_shape<S, NP, true>(p, a, sm_count, st)
-                : launch_shape<S, NP, false>(p, a, sm_count, st);
+  // the FP64 copy of W fits next to three operand stages up to No = 24
+  const bool wsmem = a.No <= 24;
+  if (wsmem)
+    return split0 ? launch_shape<S, NP, true, true>(p, a, sm_count, st)
+                  : launch_shape<S, NP, false, true>(p, a, sm_count, st);
+  return split0 ? launch_shape<S, NP, true, false>(p, a, sm_count, st)
+                : launch_shape<S, NP, false, false>(p, a, sm_count, st);
 }
 
 template <int S>
