@@ -70,6 +70,7 @@ enum : int {
 
 struct SplitMaps {
   CUtensorMap TaN, TaT, VhN, VhT, Vp, TpN, TpT;
+  CUtensorMap JhN, JhT, Jp;  // (cT) intermediates in place of V_hhhp, V_pphp
 };
 
 struct SplitArgs {
@@ -80,7 +81,8 @@ struct SplitArgs {
   int n_triples;
   int64_t t_begin, t_end;
   unsigned long long *queue;
-  double tai_sign, unit;
+  double tai_sign, unit, unit_j;
+  int use_j;  // second pass with the J intermediates ((cT) energy)
   double *e, *ect;
   int *status;
   float *wglobal;  // two W buffers per CTA (one 8-byte cell per element)
@@ -143,7 +145,8 @@ struct Part {
 
 // Operand sources of group g, part pt (0 nat particle, 1 nat hole,
 // 2 transposed particle, 3 transposed hole) for tuple (a,b,c).
-__device__ __forceinline__ Part part_of(const SplitMaps &m, int g, int pt, int a, int b, int c) {
+__device__ __forceinline__ Part part_of(const SplitMaps &m, int g, int pt, int a, int b, int c,
+                                        int pass) {
   // per group: natural (x, w, (y,z), hole (u,v), holeT), transposed likewise
   int x, w, y, z, u, v, holeT;
   const bool tr = pt >= 2;
@@ -162,11 +165,11 @@ __device__ __forceinline__ Part part_of(const SplitMaps &m, int g, int pt, int a
   if (p.particle) {
     p.amap = tr ? &m.TaT : &m.TaN;
     p.ax = x;
-    p.bmap = &m.Vp;
+    p.bmap = pass ? &m.Jp : &m.Vp;
     p.bz = z;
     p.by = y;
   } else {
-    p.amap = tr ? &m.VhT : &m.VhN;
+    p.amap = pass ? (tr ? &m.JhT : &m.JhN) : (tr ? &m.VhT : &m.VhN);
     p.ax = w;
     p.bmap = holeT ? &m.TpT : &m.TpN;
     p.bz = v;
@@ -219,7 +222,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int No = g.No, No2 = No * No, No3 = No2 * No;
   const int kStages = g.nstages;
   unsigned char *tail = ring + kStages * K::kStageBytes;
-  double *Wbase = reinterpret_cast<double *>(g.wglobal) + (size_t)blockIdx.x * 2 * No3;
+  // W buffers: [tuple parity][pass] per CTA, pass 1 = J intermediates
+  const int npass = g.use_j ? 2 : 1;
+  double *Wbase = reinterpret_cast<double *>(g.wglobal) + (size_t)blockIdx.x * 2 * npass * No3;
   uint64_t *full = reinterpret_cast<uint64_t *>(tail);
   uint64_t *empty = full + kMaxStages;
   uint64_t *accf = empty + kMaxStages;
@@ -262,6 +267,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     prefetch_tensormap(&maps.Vp);
     prefetch_tensormap(&maps.TpN);
     prefetch_tensormap(&maps.TpT);
+    if (g.use_j) {
+      prefetch_tensormap(&maps.JhN);
+      prefetch_tensormap(&maps.JhT);
+      prefetch_tensormap(&maps.Jp);
+    }
   }
   // rows of the A stage tiles past No*jt are never written by TMA: zero them
   for (int i = threadIdx.x; i < kStages * K::kStageBytes / 16; i += kThreads)
@@ -302,11 +312,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         tslot[ts] = s;
         mbar_arrive(&tfull[ts]);  // release: the slot is visible to the waiters
         if (stop) break;
-        for (int grp = 0; grp < 3 && alive; ++grp)
+        for (int gi = 0; gi < 3 * npass && alive; ++gi)
           for (int mt = 0; mt < ntiles && alive; ++mt) {
-            const int j0 = mt * jt;
+            const int j0 = mt * jt, grp = gi % 3, pass = gi / 3;
             for (int pt = 0; pt < 4 && alive; ++pt) {
-              const Part p = part_of(maps, grp, pt, s.a, s.b, s.c);
+              const Part p = part_of(maps, grp, pt, s.a, s.b, s.c, pass);
               const int nch = p.particle ? kch : 1;
               for (int ch = 0; ch < nch && alive; ++ch)
                 for (int sa = 0; sa < S; ++sa) {
@@ -341,7 +351,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int64_t t = tslot[ts].t;
         mbar_arrive(&tempty[ts]);
         if (t < 0) break;
-        for (int it = 0; it < 3 * ntiles && alive; ++it) {
+        for (int it = 0; it < 3 * npass * ntiles && alive; ++it) {
           const int buf = item_count % K::kNbuf;
           const uint32_t use = item_count / K::kNbuf;
           if (use > 0 && !mbar_wait(&acce[buf], (use - 1) & 1, g.status, kErrTimeoutAccEmpty)) {
@@ -418,9 +428,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int wb = k & 1;
       const uint32_t wuse = k >> 1;
       ok = wuse == 0 || mbar_wait(&wfree[wb], (wuse - 1) & 1, g.status, kErrTimeoutEmpty);
-      int2 *Wc = reinterpret_cast<int2 *>(Wbase + (size_t)wb * No3);
-      for (int it = 0; it < 3 * ntiles; ++it) {
-        const int grp = it / ntiles, mt = it % ntiles;
+      for (int it = 0; it < 3 * npass * ntiles; ++it) {
+        const int gi = it / ntiles, mt = it % ntiles, grp = gi % 3, pass = gi / 3;
+        int2 *Wc = reinterpret_cast<int2 *>(Wbase + (size_t)(wb * npass + pass) * No3);
         const int buf = item_count % K::kNbuf;
         const uint32_t use = item_count / K::kNbuf;
         bool okw = ok && alive && mbar_wait(&accf[buf], use & 1, g.status, kErrTimeoutAccFull);
@@ -518,7 +528,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (er < No) esm[er] = g.epsi[er];
       const int wb = k & 1;
       ok = mbar_wait(&wfull[wb], (k >> 1) & 1, g.status, kErrTimeoutAccFull);
-      double *Wg = Wbase + (size_t)wb * No3;
+      double *Wg = Wbase + (size_t)(wb * npass) * No3;
       int2 *Wc = reinterpret_cast<int2 *>(Wg);
       // W = unit * (level-0 integer + rest) in FP64: copied into shared
       // memory (the buffer is zeroed and handed back to the epilogue at
@@ -532,7 +542,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       __threadfence_block();
       named_bar_sync(2, kEnergyThreads);
-      if (WSMEM && er == 0) mbar_arrive(&wfree[wb]);
+      if (WSMEM && !g.use_j && er == 0) mbar_arrive(&wfree[wb]);
 
       int cls = 0;  // src/atrip/Atrip.cxx:640-642
       if (a == b) cls++;
@@ -548,46 +558,65 @@ __global__ void __launch_bounds__(kThreads, 1)
         z += tc[kx] * Vab[i + j * No];
         return z;
       };
-      double sum = 0.0;
-      for (int n = er; n < g.n_triples && ok; n += kEnergyThreads) {
-        const uint32_t tp = g.triples[n];
-        const int i = tp & 0xff, j = (tp >> 8) & 0xff, kx = (tp >> 16) & 0xff;
-        const double facjk = j == kx ? 0.5 : 1.0, facij = i == j ? 0.5 : 1.0;
-        const double denominator = epsabc - ((esm[i] + esm[j]) + esm[kx]);
-        double value;
-        if (distinct) {
-          const double U = Zv(i, j, kx), V = Zv(i, kx, j), Wv = Zv(j, i, kx), X = Zv(j, kx, i),
-                       Y = Zv(kx, i, j), Z = Zv(kx, j, i);
-          const double A = W(i, j, kx), B = W(i, kx, j), C = W(j, i, kx), D = W(j, kx, i),
-                       E = W(kx, i, j), F = W(kx, j, i);
-          const double UXY = U + (X + Y), VWZ = V + (Wv + Z), ADE = A + (D + E),
-                       BCF = B + (C + F);
-          const double first = A * U + (B * V + (C * Wv + (D * X + (E * Y + F * Z))));
-          value = 3.0 * first + ((UXY - 2.0 * VWZ) * ADE + (VWZ - 2.0 * UXY) * BCF);
-        } else {
-          const double U = Zv(i, j, kx), V = Zv(j, kx, i), Wv = Zv(kx, i, j);
-          const double A = W(i, j, kx), B = W(j, kx, i), C = W(kx, i, j);
-          value = 3.0 * ((A * U + B * V) + C * Wv) - (A + (B + C)) * (U + (V + Wv));
+      // one tuple energy (src/atrip/Equations.cxx:101-238) with T values
+      // from Tv and Z = W + singles; reduced over the energy warps
+      auto tuple_energy = [&](auto &&Tv) {
+        double sum = 0.0;
+        for (int n = er; n < g.n_triples && ok; n += kEnergyThreads) {
+          const uint32_t tp = g.triples[n];
+          const int i = tp & 0xff, j = (tp >> 8) & 0xff, kx = (tp >> 16) & 0xff;
+          const double facjk = j == kx ? 0.5 : 1.0, facij = i == j ? 0.5 : 1.0;
+          const double denominator = epsabc - ((esm[i] + esm[j]) + esm[kx]);
+          double value;
+          if (distinct) {
+            const double U = Zv(i, j, kx), V = Zv(i, kx, j), Wv = Zv(j, i, kx),
+                         X = Zv(j, kx, i), Y = Zv(kx, i, j), Z = Zv(kx, j, i);
+            const double A = Tv(i, j, kx), B = Tv(i, kx, j), C = Tv(j, i, kx), D = Tv(j, kx, i),
+                         E = Tv(kx, i, j), F = Tv(kx, j, i);
+            const double UXY = U + (X + Y), VWZ = V + (Wv + Z), ADE = A + (D + E),
+                         BCF = B + (C + F);
+            const double first = A * U + (B * V + (C * Wv + (D * X + (E * Y + F * Z))));
+            value = 3.0 * first + ((UXY - 2.0 * VWZ) * ADE + (VWZ - 2.0 * UXY) * BCF);
+          } else {
+            const double U = Zv(i, j, kx), V = Zv(j, kx, i), Wv = Zv(kx, i, j);
+            const double A = Tv(i, j, kx), B = Tv(j, kx, i), C = Tv(kx, i, j);
+            value = 3.0 * ((A * U + B * V) + C * Wv) - (A + (B + C)) * (U + (V + Wv));
+          }
+          sum += (2.0 * value / denominator) * (facjk * facij);
         }
-        sum += (2.0 * value / denominator) * (facjk * facij);
-      }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-      if (lane == 0) red[er >> 5] = sum;
-      named_bar_sync(2, kEnergyThreads);
-      if (er == 0) {
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (lane == 0) red[er >> 5] = sum;
+        named_bar_sync(2, kEnergyThreads);
         double e = 0.0;
         for (int w = 0; w < kEnergyWarps; ++w) e += red[w];
+        named_bar_sync(2, kEnergyThreads);  // red is reused
+        return e;
+      };
+      const double e = tuple_energy(W);
+      double ect = e;
+      if (g.use_j) {
+        // (cT): T from the J pass, Z as above (src/atrip/Atrip.cxx:928-963)
+        int2 *WJc = reinterpret_cast<int2 *>(Wbase + (size_t)(wb * npass + 1) * No3);
+        const double uj = g.unit_j;
+        ect = tuple_energy([&](int i, int j, int kx) {
+          const int2 cell = WJc[i + No * (j + No * kx)];
+          return uj * ((double)cell.x + (double)__int_as_float(cell.y));
+        });
+        for (int i = er; i < No3; i += kEnergyThreads) WJc[i] = make_int2(0, 0);
+        __threadfence_block();
+      }
+      if (er == 0) {
         g.e[s.t] = e;
-        g.ect[s.t] = e;
+        g.ect[s.t] = ect;
       }
       if (!WSMEM) {
         // zero the buffer for the tuple after next, then release it
         for (int i = er; i < No3; i += kEnergyThreads) Wd[i] = 0.0;
         __threadfence_block();
       }
-      named_bar_sync(2, kEnergyThreads);  // Wsm / red reused by the next tuple
-      if (!WSMEM && er == 0) mbar_arrive(&wfree[wb]);
+      named_bar_sync(2, kEnergyThreads);  // Wsm is reused by the next tuple
+      if ((!WSMEM || g.use_j) && er == 0) mbar_arrive(&wfree[wb]);
     }
     __syncwarp();
   }
@@ -605,7 +634,10 @@ struct SplitImpl {
   int S = 0, No = 0, Nv = 0, Ep = 0;
   __nv_bfloat16 *TaS = nullptr, *TaST = nullptr, *VhS = nullptr, *VhST = nullptr,
                 *VpS = nullptr, *TpS = nullptr, *TpTS = nullptr;
-  double unit = 1.0;
+  __nv_bfloat16 *JhS = nullptr, *JhST = nullptr, *JpS = nullptr;  // (cT), cut on demand
+  bool has_j = false;
+  int eT = 0;
+  double unit = 1.0, unit_j = 1.0;
   float *wglobal = nullptr;
   size_t wglobal_floats = 0;
   int *d_status = nullptr;
@@ -621,6 +653,9 @@ void free_impl(SplitImpl *p) {
   cudaFree(p->VpS);
   cudaFree(p->TpS);
   cudaFree(p->TpTS);
+  cudaFree(p->JhS);
+  cudaFree(p->JhST);
+  cudaFree(p->JpS);
   cudaFree(p->wglobal);
   cudaFree(p->d_status);
   delete p;
@@ -708,6 +743,7 @@ int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, cudaSt
   if (rc != ATRIP_OK) return rc;
   *launches += 3;
   const int eT = exponent_of(mT), eV = exponent_of(mVp > mVh ? mVp : mVh);
+  p->eT = eT;
   p->unit = std::ldexp(1.0, eT + eV - 14);
   const double sT = std::ldexp(1.0, 7 - eT), sV = std::ldexp(1.0, 7 - eV);
 
@@ -781,6 +817,59 @@ int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, cudaSt
     if ((rc = make_map(&p->maps.TpN, p->TpS, d, box))) return rc;
     if ((rc = make_map(&p->maps.TpT, p->TpTS, d, box))) return rc;
   }
+  p->maps.JhN = p->maps.VhN;
+  p->maps.JhT = p->maps.VhT;
+  p->maps.Jp = p->maps.Vp;
+  return ATRIP_OK;
+}
+
+// Digit slices and maps of the (cT) intermediates, with their own scale.
+int prepare_j(SplitImpl *p, const DeviceTensors &dt, cudaStream_t st, int64_t *launches) {
+  const int No = p->No, Nv = p->Nv, S = p->S;
+  const int64_t No2 = (int64_t)No * No, Ep = p->Ep;
+  unsigned long long *d_tmp = nullptr;
+  ATRIP_CUDA_TRY(cudaMalloc(&d_tmp, sizeof(unsigned long long)));
+  double mJp = 0, mJh = 0;
+  int rc = absmax(dt.Jpt, (int64_t)Nv * Nv * No * Nv, d_tmp, st, &mJp);
+  if (rc == ATRIP_OK) rc = absmax(dt.Jht, (int64_t)Nv * No2 * No, d_tmp, st, &mJh);
+  cudaFree(d_tmp);
+  if (rc != ATRIP_OK) return rc;
+  *launches += 2;
+  const int eJ = exponent_of(mJp > mJh ? mJp : mJh);
+  p->unit_j = std::ldexp(1.0, p->eT + eJ - 14);
+  const double sJ = std::ldexp(1.0, 7 - eJ);
+  const size_t nVh = (size_t)S * Nv * No2 * kHoleK, nVp = (size_t)S * Nv * Nv * No * Ep;
+  ATRIP_CUDA_TRY(cudaMalloc(&p->JhS, 2 * nVh));
+  ATRIP_CUDA_TRY(cudaMalloc(&p->JhST, 2 * nVh));
+  ATRIP_CUDA_TRY(cudaMalloc(&p->JpS, 2 * nVp));
+  SliceJob j;
+  j.S = S;
+  j.sign = 1.0;
+  j.src = dt.Jht; j.dst = p->JhS; j.nrows = Nv * No2; j.n1 = No; j.n2 = No;
+  j.so = No2 * No; j.s1 = No2; j.s2 = No; j.sk = 1; j.K = No; j.Kp = kHoleK; j.scale = sJ;
+  if ((rc = run_slices(j, st))) return rc;
+  j.dst = p->JhST; j.s1 = No; j.s2 = No2;
+  if ((rc = run_slices(j, st))) return rc;
+  j.src = dt.Jpt; j.dst = p->JpS; j.nrows = (int64_t)Nv * Nv * No; j.n1 = Nv; j.n2 = No;
+  j.so = (int64_t)Nv * No * Nv; j.s1 = (int64_t)No * Nv; j.s2 = Nv; j.sk = 1; j.K = Nv;
+  j.Kp = (int)Ep; j.scale = sJ;
+  if ((rc = run_slices(j, st))) return rc;
+  *launches += 3;
+  ATRIP_CUDA_TRY(cudaStreamSynchronize(st));
+  const int jt = 128 / No;
+  const int NP = No <= 16 ? 16 : No <= 32 ? 32 : No <= 48 ? 48 : 64;
+  {
+    const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt, 1, 1};
+    if ((rc = make_map(&p->maps.JhN, p->JhS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.JhT, p->JhST, d, box))) return rc;
+  }
+  {
+    const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)NP, 1, 1, 1};
+    if ((rc = make_map(&p->maps.Jp, p->JpS, d, box))) return rc;
+  }
+  p->has_j = true;
   return ATRIP_OK;
 }
 
@@ -849,10 +938,6 @@ int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_cou
     set_error("split form: slices must be 2, 3 or 4");
     return ATRIP_ERR_ARGUMENT;
   }
-  if (use_j) {
-    set_error("split form: the (cT) intermediates are only supported by the FP64 form");
-    return ATRIP_ERR_UNSUPPORTED;
-  }
   if (!s.valid || s.slices != slices || !s.impl) {
     split_free(s);
     auto *p = new SplitImpl();
@@ -866,9 +951,14 @@ int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_cou
     s.slices = slices;
   }
   auto *p = static_cast<SplitImpl *>(s.impl);
+  if (use_j && !p->has_j) {
+    const int rc = prepare_j(p, dt, st, launches);
+    if (rc != ATRIP_OK) return rc;
+  }
   {
-    // two W buffers (one double per element) per CTA, zeroed before launch
-    const size_t need = (size_t)sm_count * 2 * 2 * No * No * No;  // in floats
+    // W buffers (one double per element): two tuple parities x passes per
+    // CTA, zeroed before launch
+    const size_t need = (size_t)sm_count * 2 * (use_j ? 2 : 1) * 2 * No * No * No;  // floats
     if (need > p->wglobal_floats) {
       cudaFree(p->wglobal);
       p->wglobal = nullptr;
@@ -896,6 +986,8 @@ int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_cou
   a.queue = queue;
   a.tai_sign = tai_sign;
   a.unit = p->unit;
+  a.unit_j = p->unit_j;
+  a.use_j = use_j ? 1 : 0;
   a.e = e;
   a.ect = ect;
   a.status = p->d_status;

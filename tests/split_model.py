@@ -38,38 +38,55 @@ def digit_components(x: np.ndarray, e: int, S: int):
     return out
 
 
-def split_tuple_energies(d: dict, S: int, t0: int = 0, t1: int | None = None):
-    """Per-tuple energies of the split form's arithmetic with S slices."""
-    No, Nv = d["No"], d["Nv"]
-    eT = exponent(float(np.max(np.abs(d["Tabij"]))))
-    eV = exponent(max(float(np.max(np.abs(d["Vabci"]))), float(np.max(np.abs(d["Vijka"])))))
-    Tc = digit_components(d["Tabij"], eT, S)
-    Vpc = digit_components(d["Vabci"], eV, S)
-    Vhc = digit_components(d["Vijka"], eV, S)
-    problems = []
+def _problems(d, Tc, Pc, Hc, S, pkey, hkey):
+    out = []
     for p in range(S):
         m = S - p
         dd = dict(d)
         dd["Tabij"] = np.asfortranarray(Tc[p])
-        dd["Vabci"] = np.asfortranarray(sum(Vpc[:m]))
-        dd["Vijka"] = np.asfortranarray(sum(Vhc[:m]))
-        problems.append(oracle.Problem(dd))
+        dd["Vabci"] = np.asfortranarray(sum(Pc[:m]))
+        dd["Vijka"] = np.asfortranarray(sum(Hc[:m]))
+        out.append(oracle.Problem(dd))
+    return out
+
+
+def split_tuple_energies(d: dict, S: int, t0: int = 0, t1: int | None = None,
+                         use_j: bool = False):
+    """Per-tuple energies of the split form's arithmetic with S slices;
+    with use_j also the (cT) energies (T from the J intermediates, Z from
+    V), returned as (e, ect)."""
+    No, Nv = d["No"], d["Nv"]
+    eT = exponent(float(np.max(np.abs(d["Tabij"]))))
+    eV = exponent(max(float(np.max(np.abs(d["Vabci"]))), float(np.max(np.abs(d["Vijka"])))))
+    Tc = digit_components(d["Tabij"], eT, S)
+    problems = _problems(d, Tc, digit_components(d["Vabci"], eV, S),
+                         digit_components(d["Vijka"], eV, S), S, "Vabci", "Vijka")
+    jproblems = []
+    if use_j:
+        eJ = exponent(max(float(np.max(np.abs(d["Jabci"]))), float(np.max(np.abs(d["Jijka"])))))
+        jproblems = _problems(d, Tc, digit_components(d["Jabci"], eJ, S),
+                              digit_components(d["Jijka"], eJ, S), S, "Jabci", "Jijka")
     full = oracle.Problem(d)
     lst = oracle.tuple_list(Nv)
     t1 = len(lst) if t1 is None else t1
     lib = oracle._load()
     out = np.zeros(t1 - t0)
+    out_ct = np.zeros(t1 - t0)
+    eps = np.ascontiguousarray(d["epsi"], dtype=np.float64)
     for n, t in enumerate(range(t0, t1)):
         a, b, c = (int(v) for v in lst[t])
         W = np.zeros(No ** 3)
         for pr in problems:
-            Tp, _ = oracle.tuple_arrays(pr, a, b, c)
-            W += Tp
+            W += oracle.tuple_arrays(pr, a, b, c)[0]
         # Z = W + singles, from the full-precision problem
         T_full, Z_full = oracle.tuple_arrays(full, a, b, c)
         Z = W + (Z_full - T_full)
         epsabc = d["epsa"][a] + d["epsa"][b] + d["epsa"][c]
-        eps = np.ascontiguousarray(d["epsi"], dtype=np.float64)
         fn = lib.oracle_energy_distinct if (a != b and b != c) else lib.oracle_energy_same
         out[n] = fn(float(epsabc), No, eps.ctypes.data, W.ctypes.data, Z.ctypes.data)
-    return out
+        if use_j:
+            WJ = np.zeros(No ** 3)
+            for pr in jproblems:
+                WJ += oracle.tuple_arrays(pr, a, b, c)[0]
+            out_ct[n] = fn(float(epsabc), No, eps.ctypes.data, WJ.ctypes.data, Z.ctypes.data)
+    return (out, out_ct) if use_j else out

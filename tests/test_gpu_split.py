@@ -71,14 +71,33 @@ def test_split_scaled_twin_meets_1e8_hartree():
     assert abs(e3 - e64) <= 1e-8, abs(e3 - e64)
 
 
-def test_split_rejects_ct_and_bad_slices():
-    d = synth.make_inputs(4, 7, 1, with_j=True)
+@pytest.mark.parametrize("No,Nv,seed", [(5, 9, 3), (8, 20, 1), (24, 14, 2), (30, 12, 6)])
+def test_split_ct_energy(No, Nv, seed):
+    """(cT): the J pass reproduces the model and stays within the 3-slice
+    bound of the FP64 form's ct_energy."""
+    d = synth.make_inputs(No, Nv, seed, with_j=True)
+    n = min(synth.n_tuples(Nv), 80)
+    model_e, model_ct = split_model.split_tuple_energies(d, 3, 0, n, use_j=True)
     with _ctx(d) as ctx:
         ctx.upload("Jijka", d["Jijka"])
         ctx.upload("Jabci", d["Jabci"])
-        with pytest.raises(capi.AtripError) as ei:
-            ctx.run(form="split_bf16", slices=3, use_j=True)
-        assert ei.value.status == capi.ERR_UNSUPPORTED
+        r64 = ctx.run(form="fp64", use_j=True, max_iterations=n - 1)
+        e64, ect64 = ctx.tuple_energies(0, n)
+        r = ctx.run(form="split_bf16", slices=3, use_j=True, max_iterations=n - 1)
+        e, ect = ctx.tuple_energies(0, n)
+        # the same context still runs without the J pass afterwards
+        r2 = ctx.run(form="split_bf16", slices=3, use_j=False, max_iterations=n - 1)
+    scale = np.max(np.abs(model_e))
+    assert np.max(np.abs(e - model_e)) <= 1e-7 * scale
+    assert np.max(np.abs(ect - model_ct)) <= 1e-7 * scale
+    assert np.max(np.abs(ect - ect64)) <= BOUND[3] * np.max(np.abs(e64))
+    assert abs(r.ct_energy - r64.ct_energy) <= BOUND[3] * abs(r64.energy)
+    assert r2.energy == r.energy and r2.ct_energy == r2.energy
+
+
+def test_split_rejects_bad_slices():
+    d = synth.make_inputs(4, 7, 1)
+    with _ctx(d) as ctx:
         with pytest.raises(capi.AtripError) as ei:
             ctx.run(form="split_bf16", slices=5, use_j=False)
         assert ei.value.status == capi.ERR_ARGUMENT
