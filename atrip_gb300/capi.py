@@ -25,7 +25,8 @@ EXPORTED = [
     "atrip_gpu_create", "atrip_gpu_upload", "atrip_gpu_upload_device", "atrip_gpu_release",
     "atrip_gpu_run", "atrip_gpu_tuple_energies", "atrip_gpu_n_tuples", "atrip_gpu_tuple_at",
     "atrip_gpu_destroy", "atrip_gpu_last_error", "atrip_gpu_version", "atrip_gpu_measure_peaks",
-    "atrip_gpu_run_fp64_noalloc",
+    "atrip_gpu_run_fp64_noalloc", "atrip_gpu_batch_create", "atrip_gpu_batch_run",
+    "atrip_gpu_batch_destroy", "atrip_gpu_batch_plan",
 ]
 
 
@@ -97,6 +98,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(DeviceInputs), ctypes.c_int64,
         ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
         ctypes.c_void_p, ctypes.c_void_p]
+    lib.atrip_gpu_batch_create.argtypes = [P, ctypes.c_int32, ctypes.POINTER(P)]
+    lib.atrip_gpu_batch_run.argtypes = [P, ctypes.POINTER(RunOptions), P]
+    lib.atrip_gpu_batch_destroy.argtypes = [P]
+    lib.atrip_gpu_batch_plan.argtypes = [P, P, ctypes.c_int32, P]
     for name in EXPORTED:
         if name not in ("atrip_gpu_n_tuples", "atrip_gpu_last_error", "atrip_gpu_version"):
             getattr(lib, name).restype = ctypes.c_int
@@ -178,6 +183,53 @@ class Context:
     def close(self) -> None:
         if getattr(self, "h", None):
             self.lib.atrip_gpu_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_plan(no, nv):
+    """Launch order (cost-descending, stable) the batch gives these sizes."""
+    import numpy as np
+    no = np.ascontiguousarray(no, dtype=np.int32)
+    nv = np.ascontiguousarray(nv, dtype=np.int32)
+    order = np.zeros(max(no.size, 1), dtype=np.int32)
+    check(load().atrip_gpu_batch_plan(no.ctypes.data, nv.ctypes.data, no.size, order.ctypes.data))
+    return order[:no.size]
+
+
+class Batch:
+    """Several contexts run together (wraps atrip_gpu_batch)."""
+
+    def __init__(self, contexts):
+        self.lib = load()
+        self.contexts = list(contexts)
+        arr = (ctypes.c_void_p * len(self.contexts))(*[c.h.value for c in self.contexts])
+        h = ctypes.c_void_p()
+        check(self.lib.atrip_gpu_batch_create(arr, len(self.contexts), ctypes.byref(h)))
+        self.h = h
+
+    def run(self, form: str = "fp64", slices: int = 0, ijkabc: bool = False, use_j: bool = True,
+            first_iteration: int = 0, max_iterations: int = 0, stream: int = 0):
+        opts = RunOptions(FORMS[form], slices, int(ijkabc), int(use_j), first_iteration,
+                          max_iterations, 0.0, ctypes.c_void_p(stream or None))
+        res = (Result * len(self.contexts))()
+        check(self.lib.atrip_gpu_batch_run(self.h, ctypes.byref(opts), res))
+        return list(res)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.atrip_gpu_batch_destroy(self.h)
             self.h = None
 
     def __enter__(self):

@@ -9,6 +9,7 @@
 #include "atrip_gb300.h"
 #include "engine.cuh"
 #include "split.cuh"
+#include "context.cuh"
 
 namespace atrip_gb300 {
 
@@ -19,25 +20,6 @@ void clear_error() { g_last_error.clear(); }
 }  // namespace atrip_gb300
 
 using namespace atrip_gb300;
-
-struct atrip_gpu_context {
-  int No = 0, Nv = 0, device = 0, sm_count = 0;
-  int64_t n_tuples = 0;
-  int n_triples = 0;
-  bool have[ATRIP_N_TENSORS] = {};
-  DeviceTensors dt;
-  uint32_t *d_tuples = nullptr;
-  uint32_t *d_triples = nullptr;
-  double *d_e = nullptr, *d_ect = nullptr;
-  int64_t e_lo = 0, e_hi = 0;  // tuple range holding energies of the last run
-  double *d_workspace = nullptr;
-  size_t workspace_doubles = 0;
-  unsigned long long *d_queue = nullptr;
-  double *d_partials = nullptr, *d_sum = nullptr;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  SplitState split;
-};
 
 namespace {
 

@@ -53,7 +53,21 @@ struct TriplesArgs {
 };
 
 cudaError_t launch_triples_fp64(const TriplesArgs &a, int grid, cudaStream_t s);
+
+// Several systems in one persistent launch (systems[] and prefix[] in device
+// memory; prefix[n] = total tuples; workspace ws_stride doubles per CTA).
+struct BatchArgs {
+  const TriplesArgs *systems;
+  const int64_t *prefix;
+  int n;
+  unsigned long long *queue;
+  double *workspace;
+  int64_t ws_stride;
+};
+cudaError_t launch_triples_fp64_batch(const BatchArgs &b, int max_no, int grid, cudaStream_t s);
+cudaError_t launch_batch_energy_sum(const BatchArgs &b, double *sums, cudaStream_t s);
 int triples_fp64_max_blocks_per_sm(int No);
+int triples_fp64_batch_max_blocks_per_sm(int max_no);
 
 // dst[i0 + n0 (i1 + n1 (i2 + n2 i3))] = src[i0 s0 + i1 s1 + i2 s2 + i3 s3]
 cudaError_t launch_permute4(double *dst, const double *src, const int64_t n[4],

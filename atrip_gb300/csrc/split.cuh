@@ -13,10 +13,24 @@ struct SplitState {
   bool valid = false;  // pre-split operands match the uploaded tensors
   int slices = 0;
   void *impl = nullptr;
+  uint64_t generation = 0;  // bumped whenever device buffers are (re)allocated
 };
 
 void split_invalidate(SplitState &s);
 void split_free(SplitState &s);
+
+// Cut the digit slices and build the tensor maps (host work, allocations).
+int split_prepare(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
+                  bool use_j, int slices, cudaStream_t st, int64_t *launches);
+// Queue one launch over tuples [t_begin, t_end) on st (no host sync; may be
+// captured into a CUDA graph).  The caller zeroes *queue first.
+int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
+                  const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,
+                  int64_t t_end, double tai_sign, bool use_j, unsigned long long *queue,
+                  double *e, double *ect, cudaStream_t st, int64_t *launches);
+// Device status word of the last launch (0 = fine) and its host check.
+const int *split_status_ptr(const SplitState &s);
+int split_status_check(int status);
 
 // Runs tuples [t_begin, t_end) in the split form, writing e[t], ect[t].
 int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,

@@ -927,13 +927,11 @@ void split_free(SplitState &s) {
   free_impl(static_cast<SplitImpl *>(s.impl));
   s.impl = nullptr;
   s.valid = false;
+  s.generation++;
 }
 
-int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
-              const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,
-              int64_t t_end, double tai_sign, bool use_j, int slices,
-              unsigned long long *queue, double *e, double *ect, cudaStream_t st,
-              int64_t *launches) {
+int split_prepare(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
+                  bool use_j, int slices, cudaStream_t st, int64_t *launches) {
   if (slices < 2 || slices > 4) {
     set_error("split form: slices must be 2, 3 or 4");
     return ATRIP_ERR_ARGUMENT;
@@ -952,21 +950,33 @@ int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_cou
   }
   auto *p = static_cast<SplitImpl *>(s.impl);
   if (use_j && !p->has_j) {
+    s.generation++;
     const int rc = prepare_j(p, dt, st, launches);
     if (rc != ATRIP_OK) return rc;
   }
-  {
-    // W buffers (one double per element): two tuple parities x passes per
-    // CTA, zeroed before launch
-    const size_t need = (size_t)sm_count * 2 * (use_j ? 2 : 1) * 2 * No * No * No;  // floats
-    if (need > p->wglobal_floats) {
-      cudaFree(p->wglobal);
-      p->wglobal = nullptr;
-      ATRIP_CUDA_TRY(cudaMalloc(&p->wglobal, sizeof(float) * need));
-      p->wglobal_floats = need;
-    }
-    ATRIP_CUDA_TRY(cudaMemsetAsync(p->wglobal, 0, sizeof(float) * need, st));
+  // W buffers (one double per element): two tuple parities x passes per CTA
+  const size_t need = (size_t)sm_count * 2 * (use_j ? 2 : 1) * 2 * No * No * No;  // floats
+  if (need > p->wglobal_floats) {
+    s.generation++;
+    cudaFree(p->wglobal);
+    p->wglobal = nullptr;
+    ATRIP_CUDA_TRY(cudaMalloc(&p->wglobal, sizeof(float) * need));
+    p->wglobal_floats = need;
   }
+  return ATRIP_OK;
+}
+
+int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
+                  const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,
+                  int64_t t_end, double tai_sign, bool use_j, unsigned long long *queue,
+                  double *e, double *ect, cudaStream_t st, int64_t *launches) {
+  auto *p = static_cast<SplitImpl *>(s.impl);
+  if (!s.valid || !p || (use_j && !p->has_j)) {
+    set_error("split form: operands not prepared");
+    return ATRIP_ERR_STATE;
+  }
+  const size_t need = (size_t)sm_count * 2 * (use_j ? 2 : 1) * 2 * No * No * No;
+  ATRIP_CUDA_TRY(cudaMemsetAsync(p->wglobal, 0, sizeof(float) * need, st));
   ATRIP_CUDA_TRY(cudaMemsetAsync(p->d_status, 0, sizeof(int), st));
   SplitArgs a;
   a.No = No;
@@ -993,21 +1003,44 @@ int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_cou
   a.status = p->d_status;
   a.wglobal = p->wglobal;
   int rc;
-  switch (slices) {
+  switch (s.slices) {
     case 2: rc = launch_s<2>(p, a, sm_count, st); break;
     case 3: rc = launch_s<3>(p, a, sm_count, st); break;
     default: rc = launch_s<4>(p, a, sm_count, st); break;
   }
   if (rc != ATRIP_OK) return rc;
   *launches += 1;
-  int status = 0;
-  ATRIP_CUDA_TRY(cudaMemcpyAsync(&status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
-  ATRIP_CUDA_TRY(cudaStreamSynchronize(st));
+  return ATRIP_OK;
+}
+
+const int *split_status_ptr(const SplitState &s) {
+  auto *p = static_cast<SplitImpl *>(s.impl);
+  return p ? p->d_status : nullptr;
+}
+
+int split_status_check(int status) {
   if (status != 0) {
     set_error("split kernel: a bounded wait gave up (code " + std::to_string(status) + ")");
     return ATRIP_ERR_TIMEOUT;
   }
   return ATRIP_OK;
+}
+
+int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
+              const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,
+              int64_t t_end, double tai_sign, bool use_j, int slices,
+              unsigned long long *queue, double *e, double *ect, cudaStream_t st,
+              int64_t *launches) {
+  int rc = split_prepare(s, dt, No, Nv, sm_count, use_j, slices, st, launches);
+  if (rc != ATRIP_OK) return rc;
+  rc = split_enqueue(s, dt, No, Nv, sm_count, tuples, triples, n_triples, t_begin, t_end,
+                     tai_sign, use_j, queue, e, ect, st, launches);
+  if (rc != ATRIP_OK) return rc;
+  int status = 0;
+  ATRIP_CUDA_TRY(cudaMemcpyAsync(&status, split_status_ptr(s), sizeof(int),
+                                 cudaMemcpyDeviceToHost, st));
+  ATRIP_CUDA_TRY(cudaStreamSynchronize(st));
+  return split_status_check(status);
 }
 
 }  // namespace atrip_gb300

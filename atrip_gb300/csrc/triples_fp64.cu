@@ -64,7 +64,7 @@ struct Smem {
   double As[kKC][kMT + 1];
   double Bs[kKC][64 + 1];
   double red[kThreads / 32][2];
-  int tuple_slot;
+  long long tuple_slot;
 };
 
 // W (No^3, in the per-CTA workspace) = sum of the six fused terms.
@@ -194,6 +194,45 @@ __device__ double block_sum(double v, Smem &sm, int slot) {
   return r;  // valid in thread 0
 }
 
+// One tuple t of the system described by g: W (and W_J), energies e[t],
+// ect[t].  All threads of the block take part.
+template <int NC>
+__device__ void process_tuple(const TriplesArgs &g, Smem &sm, SinglesCtx &s, double *Wv,
+                              double *Wj, int64_t t) {
+  const uint32_t pk = g.tuples[t];
+  const int a = pk & 0x3ff, b = (pk >> 10) & 0x3ff, c = (pk >> 20) & 0x3ff;
+  const int No = g.No, Nv = g.Nv, No2 = No * No;
+  if (threadIdx.x < No) {
+    const int i = threadIdx.x;
+    s.ta[i] = g.tai_sign * g.tai[a + i * Nv];
+    s.tb[i] = g.tai_sign * g.tai[b + i * Nv];
+    s.tc[i] = g.tai_sign * g.tai[c + i * Nv];
+  }
+  if (threadIdx.x == 0) {
+    s.Vbc = g.Vhh + ((int64_t)b * Nv + c) * No2;
+    s.Vac = g.Vhh + ((int64_t)a * Nv + c) * No2;
+    s.Vab = g.Vhh + ((int64_t)a * Nv + b) * No2;
+  }
+  build_w<NC>(g, sm, Wv, g.Vht, g.Vpt, a, b, c);
+  // classification of src/atrip/Atrip.cxx:640-642
+  int cls = 0;
+  if (a == b) cls++;
+  if (b == c) cls--;
+  const bool distinct = cls == 0;
+  const double epsabc = g.epsa[a] + g.epsa[b] + g.epsa[c];
+  const double e = block_sum(energy_partial(g, Wv, Wv, s, distinct, epsabc), sm, 0);
+  double ect = e;
+  if (g.use_j) {
+    build_w<NC>(g, sm, Wj, g.Jht, g.Jpt, a, b, c);
+    ect = block_sum(energy_partial(g, Wj, Wv, s, distinct, epsabc), sm, 1);
+  }
+  if (threadIdx.x == 0) {
+    g.e[t] = e;
+    g.ect[t] = ect;
+  }
+  __syncthreads();
+}
+
 template <int NC>
 __global__ void __launch_bounds__(kThreads) triples_fp64_kernel(TriplesArgs g) {
   __shared__ Smem sm;
@@ -204,46 +243,105 @@ __global__ void __launch_bounds__(kThreads) triples_fp64_kernel(TriplesArgs g) {
   for (;;) {
     if (threadIdx.x == 0) {
       const unsigned long long q = atomicAdd(g.queue, 1ull);
-      sm.tuple_slot = (q < (unsigned long long)(g.t_end - g.t_begin)) ? (int)q : -1;
+      sm.tuple_slot = (q < (unsigned long long)(g.t_end - g.t_begin)) ? (long long)q : -1;
     }
     __syncthreads();
-    const int slot = sm.tuple_slot;
+    const long long slot = sm.tuple_slot;
     __syncthreads();
     if (slot < 0) break;
-    const int64_t t = g.t_begin + slot;
-    const uint32_t pk = g.tuples[t];
-    const int a = pk & 0x3ff, b = (pk >> 10) & 0x3ff, c = (pk >> 20) & 0x3ff;
-    const int No = g.No, Nv = g.Nv, No2 = No * No;
-    if (threadIdx.x < No) {
-      const int i = threadIdx.x;
-      s.ta[i] = g.tai_sign * g.tai[a + i * Nv];
-      s.tb[i] = g.tai_sign * g.tai[b + i * Nv];
-      s.tc[i] = g.tai_sign * g.tai[c + i * Nv];
+    process_tuple<NC>(g, sm, s, Wv, Wj, g.t_begin + slot);
+  }
+}
+
+// process_tuple<nc> for the system's own column count nc <= NC, so a small
+// system in a mixed batch does not pay for the largest system's tile width.
+template <int NC>
+__device__ void process_tuple_nc(int nc, const TriplesArgs &g, Smem &sm, SinglesCtx &s,
+                                 double *Wv, double *Wj, int64_t t) {
+  if constexpr (NC > 1) {
+    if (nc < NC) {
+      process_tuple_nc<NC - 1>(nc, g, sm, s, Wv, Wj, t);
+      return;
     }
+  }
+  process_tuple<NC>(g, sm, s, Wv, Wj, t);
+}
+
+// Many systems in one persistent launch: a single work-queue cursor runs over
+// the concatenated tuple ranges of all systems (prefix[s] .. prefix[s+1]);
+// each tuple is processed with its system's descriptor.
+template <int NC>
+__global__ void __launch_bounds__(kThreads) triples_fp64_batch_kernel(BatchArgs bt) {
+  __shared__ Smem sm;
+  __shared__ SinglesCtx s;
+  __shared__ TriplesArgs sg;
+  __shared__ int sys;
+  double *Wv = bt.workspace + (int64_t)blockIdx.x * bt.ws_stride;
+  double *Wj = Wv + bt.ws_stride / 2;
+  const int64_t total = bt.prefix[bt.n];
+  for (;;) {
     if (threadIdx.x == 0) {
-      s.Vbc = g.Vhh + ((int64_t)b * Nv + c) * No2;
-      s.Vac = g.Vhh + ((int64_t)a * Nv + c) * No2;
-      s.Vab = g.Vhh + ((int64_t)a * Nv + b) * No2;
-    }
-    build_w<NC>(g, sm, Wv, g.Vht, g.Vpt, a, b, c);
-    // classification of src/atrip/Atrip.cxx:640-642
-    int cls = 0;
-    if (a == b) cls++;
-    if (b == c) cls--;
-    const bool distinct = cls == 0;
-    const double epsabc = g.epsa[a] + g.epsa[b] + g.epsa[c];
-    const double e = block_sum(energy_partial(g, Wv, Wv, s, distinct, epsabc), sm, 0);
-    double ect = e;
-    if (g.use_j) {
-      build_w<NC>(g, sm, Wj, g.Jht, g.Jpt, a, b, c);
-      ect = block_sum(energy_partial(g, Wj, Wv, s, distinct, epsabc), sm, 1);
-    }
-    if (threadIdx.x == 0) {
-      g.e[t] = e;
-      g.ect[t] = ect;
+      const unsigned long long q = atomicAdd(bt.queue, 1ull);
+      long long slot = -1;
+      int lo = 0;
+      if (q < (unsigned long long)total) {
+        int hi = bt.n;  // prefix[lo] <= q < prefix[hi]
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) / 2;
+          if ((int64_t)q >= bt.prefix[mid]) lo = mid; else hi = mid;
+        }
+        slot = (long long)q - bt.prefix[lo];
+      }
+      sm.tuple_slot = slot;
+      sys = lo;
     }
     __syncthreads();
+    const long long slot = sm.tuple_slot;
+    if (slot < 0) break;
+    if (threadIdx.x == 0) sg = bt.systems[sys];
+    __syncthreads();
+    process_tuple_nc<NC>((sg.No + 7) / 8, sg, sm, s, Wv, Wj, sg.t_begin + slot);
   }
+}
+
+// Per-system compensated sums of e and ect (block s reduces system s, in a
+// fixed order): sums[2 s], sums[2 s + 1].
+__global__ void batch_energy_sum(BatchArgs bt, double *sums) {
+  __shared__ double sh[4][kThreads];
+  const TriplesArgs &g = bt.systems[blockIdx.x];
+  const int64_t n = g.t_end - g.t_begin;
+  double s0 = 0, c0 = 0, s1 = 0, c1 = 0;
+  auto neu = [](double &sv, double &cv, double x) {
+    const double t = sv + x;
+    if (fabs(sv) >= fabs(x)) cv += (sv - t) + x; else cv += (x - t) + sv;
+    sv = t;
+  };
+  for (int64_t t = threadIdx.x; t < n; t += kThreads) {
+    neu(s0, c0, g.e[g.t_begin + t]);
+    neu(s1, c1, g.ect[g.t_begin + t]);
+  }
+  sh[0][threadIdx.x] = s0;
+  sh[1][threadIdx.x] = c0;
+  sh[2][threadIdx.x] = s1;
+  sh[3][threadIdx.x] = c1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a0 = 0, b0 = 0, a1 = 0, b1 = 0;
+    for (int i = 0; i < kThreads; ++i) {
+      neu(a0, b0, sh[0][i]);
+      b0 += sh[1][i];
+      neu(a1, b1, sh[2][i]);
+      b1 += sh[3][i];
+    }
+    sums[2 * blockIdx.x] = a0 + b0;
+    sums[2 * blockIdx.x + 1] = a1 + b1;
+  }
+}
+
+template <int NC>
+cudaError_t launch_batch_nc(const BatchArgs &b, int grid, cudaStream_t st) {
+  triples_fp64_batch_kernel<NC><<<grid, kThreads, 0, st>>>(b);
+  return cudaGetLastError();
 }
 
 template <int NC>
@@ -266,6 +364,42 @@ cudaError_t launch_triples_fp64(const TriplesArgs &a, int grid, cudaStream_t s) 
     case 8: return launch_nc<8>(a, grid, s);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_triples_fp64_batch(const BatchArgs &b, int max_no, int grid, cudaStream_t s) {
+  switch ((max_no + 7) / 8) {
+    case 1: return launch_batch_nc<1>(b, grid, s);
+    case 2: return launch_batch_nc<2>(b, grid, s);
+    case 3: return launch_batch_nc<3>(b, grid, s);
+    case 4: return launch_batch_nc<4>(b, grid, s);
+    case 5: return launch_batch_nc<5>(b, grid, s);
+    case 6: return launch_batch_nc<6>(b, grid, s);
+    case 7: return launch_batch_nc<7>(b, grid, s);
+    case 8: return launch_batch_nc<8>(b, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_batch_energy_sum(const BatchArgs &b, double *sums, cudaStream_t s) {
+  batch_energy_sum<<<b.n, kThreads, 0, s>>>(b, sums);
+  return cudaGetLastError();
+}
+
+int triples_fp64_batch_max_blocks_per_sm(int max_no) {
+  int n = 0;
+  cudaError_t e = cudaErrorInvalidValue;
+  switch ((max_no + 7) / 8) {
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<1>, kThreads, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<2>, kThreads, 0); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<3>, kThreads, 0); break;
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<4>, kThreads, 0); break;
+    case 5: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<5>, kThreads, 0); break;
+    case 6: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<6>, kThreads, 0); break;
+    case 7: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<7>, kThreads, 0); break;
+    case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<8>, kThreads, 0); break;
+    default: break;
+  }
+  return e == cudaSuccess ? n : 0;
 }
 
 int triples_fp64_max_blocks_per_sm(int No) {

@@ -157,6 +157,32 @@ const char *atrip_gpu_version(void);
 int atrip_gpu_measure_peaks(int32_t device, double *fp64_tflops, double *fp32_tflops);
 
 /* ---------------------------------------------------------------------
+ * Batching form: many independent systems in one run.
+ *
+ * The reference runs one system per Atrip::run (src/atrip/Atrip.cxx:78-1111);
+ * a batch replaces a host loop of such calls over small molecules.  The
+ * FP64 form runs every system's tuples in ONE persistent launch over a
+ * shared device work queue; the split form runs one persistent launch per
+ * system.  Either sequence is captured into a CUDA graph on the first run
+ * and replayed by later runs with the same form, slice count and range.
+ *
+ * atrip_gpu_batch_create: systems[0..n-1] are contexts on one device; the
+ * batch keeps the pointers (destroy the batch before any of them).
+ * atrip_gpu_batch_run: opts as for atrip_gpu_run, applied to every system
+ * (start_energy must be 0); results[s] belongs to systems[s], its
+ * device_ms and kernel_launches cover the whole batch.  Afterwards
+ * atrip_gpu_tuple_energies works on each context as after atrip_gpu_run.
+ * atrip_gpu_batch_plan: the launch order (cost-descending, stable) the
+ * batch gives systems with these sizes; host-only, needs no device.       */
+typedef struct atrip_gpu_batch atrip_gpu_batch;
+
+int atrip_gpu_batch_create(atrip_gpu_context *const *systems, int32_t n, atrip_gpu_batch **out);
+int atrip_gpu_batch_run(atrip_gpu_batch *batch, const atrip_run_options *opts,
+                        atrip_result *results);
+int atrip_gpu_batch_destroy(atrip_gpu_batch *batch);
+int atrip_gpu_batch_plan(const int32_t *no, const int32_t *nv, int32_t n, int32_t *order);
+
+/* ---------------------------------------------------------------------
  * No-allocation variant (no counterpart in the reference).
  *
  * For hosts that cannot call cudaMalloc: codes whose own pool allocator

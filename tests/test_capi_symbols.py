@@ -49,3 +49,25 @@ def test_errors_without_gpu_are_status_codes():
     assert b"No must be" in lib.atrip_gpu_last_error()
     rc = lib.atrip_gpu_tuple_at(10, 10 ** 6, *(ctypes.byref(ctypes.c_int32()) for _ in range(3)))
     assert rc == capi.ERR_ARGUMENT
+
+
+def test_batch_plan_orders_by_cost():
+    """Host logic of the batching form: systems in descending per-tuple
+    cost, ties kept in caller order; empty input is fine."""
+    import numpy as np
+    no = [4, 20, 7, 20, 13, 4]
+    nv = [30, 33, 12, 33, 41, 30]
+    order = capi.batch_plan(no, nv)
+    assert sorted(order.tolist()) == list(range(len(no)))
+
+    def cost(i):
+        return ((no[i] ** 2 + 63) // 64) * ((no[i] + 7) // 8) * (nv[i] + no[i])
+    costs = [cost(i) for i in order]
+    assert costs == sorted(costs, reverse=True)
+    assert order.tolist().index(1) < order.tolist().index(3)  # stable
+    assert order.tolist().index(0) < order.tolist().index(5)
+    assert capi.batch_plan([], []).size == 0
+    lib = capi.load()
+    assert lib.atrip_gpu_batch_plan(None, None, 3, None) == capi.ERR_ARGUMENT
+    h = ctypes.c_void_p()
+    assert lib.atrip_gpu_batch_create(None, 0, ctypes.byref(h)) == capi.ERR_ARGUMENT
