@@ -26,7 +26,8 @@ EXPORTED = [
     "atrip_gpu_run", "atrip_gpu_tuple_energies", "atrip_gpu_n_tuples", "atrip_gpu_tuple_at",
     "atrip_gpu_destroy", "atrip_gpu_last_error", "atrip_gpu_version", "atrip_gpu_measure_peaks",
     "atrip_gpu_run_fp64_noalloc", "atrip_gpu_batch_create", "atrip_gpu_batch_run",
-    "atrip_gpu_batch_destroy", "atrip_gpu_batch_plan",
+    "atrip_gpu_batch_destroy", "atrip_gpu_batch_plan", "atrip_gpu_set_tuning",
+    "atrip_gpu_get_tuning", "atrip_gpu_batch_set_tuning",
 ]
 
 
@@ -52,6 +53,17 @@ class DeviceInputs(ctypes.Structure):
     """atrip_device_inputs: device pointers to column-major FP64 tensors."""
     _fields_ = [(n, ctypes.c_void_p) for n in
                 ("epsi", "epsa", "tai", "tabij", "vabij", "vijka", "vabci", "jijka", "jabci")]
+
+
+class Tuning(ctypes.Structure):
+    """atrip_tuning: launch parameters (zero = built-in choice)."""
+    _fields_ = [("fp64_ctas_per_sm", ctypes.c_int32), ("fp64_tile_rows", ctypes.c_int32),
+                ("tuples_per_claim", ctypes.c_int32), ("split_stages", ctypes.c_int32),
+                ("split_ctas", ctypes.c_int32), ("fp64_min_blocks", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 class Result(ctypes.Structure):
@@ -102,6 +114,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.atrip_gpu_batch_run.argtypes = [P, ctypes.POINTER(RunOptions), P]
     lib.atrip_gpu_batch_destroy.argtypes = [P]
     lib.atrip_gpu_batch_plan.argtypes = [P, P, ctypes.c_int32, P]
+    lib.atrip_gpu_set_tuning.argtypes = [P, ctypes.POINTER(Tuning)]
+    lib.atrip_gpu_get_tuning.argtypes = [P, ctypes.POINTER(Tuning)]
+    lib.atrip_gpu_batch_set_tuning.argtypes = [P, ctypes.POINTER(Tuning)]
     for name in EXPORTED:
         if name not in ("atrip_gpu_n_tuples", "atrip_gpu_last_error", "atrip_gpu_version"):
             getattr(lib, name).restype = ctypes.c_int
@@ -173,6 +188,18 @@ class Context:
         check(self.lib.atrip_gpu_run(self.h, ctypes.byref(opts), ctypes.byref(res)))
         return res
 
+    def set_tuning(self, **kw) -> None:
+        """Launch parameters (fields of atrip_tuning; unnamed fields are 0)."""
+        t = Tuning()
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        check(self.lib.atrip_gpu_set_tuning(self.h, ctypes.byref(t)))
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        check(self.lib.atrip_gpu_get_tuning(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
     def tuple_energies(self, t0: int, n: int):
         import numpy as np
         e = np.zeros(max(n, 1))
@@ -226,6 +253,14 @@ class Batch:
         res = (Result * len(self.contexts))()
         check(self.lib.atrip_gpu_batch_run(self.h, ctypes.byref(opts), res))
         return list(res)
+
+    def set_tuning(self, **kw) -> None:
+        """FP64 batch-kernel launch parameters (fp64_ctas_per_sm,
+        fp64_min_blocks, tuples_per_claim)."""
+        t = Tuning()
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        check(self.lib.atrip_gpu_batch_set_tuning(self.h, ctypes.byref(t)))
 
     def close(self) -> None:
         if getattr(self, "h", None):

@@ -48,6 +48,8 @@ struct atrip_gpu_batch {
   cudaGraphExec_t exec = nullptr;
   std::vector<uintptr_t> key;
   int64_t graph_launches = 0;
+  atrip_tuning tune = {};  // FP64 batch-kernel launch parameters
+  int max_per_sm = 1;      // CTAs per SM the workspace is sized for
 };
 
 namespace {
@@ -63,6 +65,10 @@ double tuple_cost(int no, int nv) {
   const double tiles = (double)((no * no + 63) / 64);
   const double cols = (double)((no + 7) / 8);
   return tiles * cols * (double)(nv + no);
+}
+
+int split_ctas(const atrip_gpu_context *c) {
+  return c->tune.split_ctas > 0 ? std::min(c->sm_count, (int)c->tune.split_ctas) : c->sm_count;
 }
 
 void destroy_graph(atrip_gpu_batch *b) {
@@ -105,6 +111,9 @@ void fill_table(atrip_gpu_batch *b, int64_t first, int64_t max_it, double tai_si
     a.e = c->d_e;
     a.ect = c->d_ect;
     a.workspace = nullptr;
+    a.rows_tile = c->tune.fp64_tile_rows == 32 ? 32 : 64;
+    a.claim = 1;
+    a.min_blocks = 0;
     prefix[k + 1] = prefix[k] + (t_end - t_begin);
   }
 }
@@ -133,6 +142,8 @@ int atrip_gpu_batch_create(atrip_gpu_context *const *systems, int32_t n, atrip_g
     if (!systems[s]) return fail(ATRIP_ERR_ARGUMENT, "null system " + std::to_string(s));
     if (systems[s]->device != systems[0]->device)
       return fail(ATRIP_ERR_ARGUMENT, "systems live on different devices");
+    if (systems[s]->No > kBatchMaxNo)
+      return fail(ATRIP_ERR_UNSUPPORTED, "batch systems need No <= " + std::to_string(kBatchMaxNo));
     for (int t = 0; t < s; ++t)
       if (systems[t] == systems[s])
         return fail(ATRIP_ERR_ARGUMENT, "system " + std::to_string(s) + " listed twice");
@@ -172,11 +183,13 @@ int atrip_gpu_batch_create(atrip_gpu_context *const *systems, int32_t n, atrip_g
   BATCH_TRY(cudaMalloc(&b->d_sums, sizeof(double) * 2 * n));
   BATCH_TRY(cudaMallocHost(&b->h_sums, sizeof(double) * 2 * n));
   BATCH_TRY(cudaMallocHost(&b->h_status, sizeof(int) * n));
-  const int per_sm = std::max(1, triples_fp64_batch_max_blocks_per_sm(b->max_no));
-  b->grid = b->sm_count * per_sm;
+  b->max_per_sm = std::max({1, triples_fp64_batch_max_blocks_per_sm(b->max_no, 0),
+                            triples_fp64_batch_max_blocks_per_sm(b->max_no, 2)});
+  b->grid = b->sm_count * std::max(1, triples_fp64_batch_max_blocks_per_sm(b->max_no, 0));
   const int64_t No = b->max_no;
   b->ws_stride = 2 * No * No * No;
-  BATCH_TRY(cudaMalloc(&b->d_workspace, sizeof(double) * b->ws_stride * b->grid));
+  BATCH_TRY(cudaMalloc(&b->d_workspace,
+                       sizeof(double) * b->ws_stride * b->sm_count * b->max_per_sm));
 #undef BATCH_TRY
   *out = b;
   return ATRIP_OK;
@@ -213,20 +226,24 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
 
   // What the captured graph depends on besides the table (copied at replay).
   std::vector<uintptr_t> key = {(uintptr_t)form, (uintptr_t)(form == ATRIP_FORM_FP64 ? 0 : slices),
-                                (uintptr_t)prefix[n]};
+                                (uintptr_t)prefix[n], (uintptr_t)b->grid,
+                                (uintptr_t)b->tune.fp64_min_blocks,
+                                (uintptr_t)b->tune.tuples_per_claim};
   if (form == ATRIP_FORM_SPLIT_BF16) {
     for (int k = 0; k < n; ++k) {
       atrip_gpu_context *c = b->sys[b->order[k]];
       const TriplesArgs &a = b->h_table[k];
-      int rc = split_prepare(c->split, c->dt, c->No, c->Nv, c->sm_count, a.use_j != 0, slices, st,
-                             &prep_launches);
+      c->split.stage_cap = c->tune.split_stages;
+      int rc = split_prepare(c->split, c->dt, c->No, c->Nv, split_ctas(c), a.use_j != 0, slices,
+                             st, &prep_launches);
       if (rc != ATRIP_OK) return rc;
       const uintptr_t more[] = {(uintptr_t)c->split.generation, (uintptr_t)c->split.impl,
                                 (uintptr_t)a.epsi, (uintptr_t)a.epsa, (uintptr_t)a.tai,
                                 (uintptr_t)a.Vhh, (uintptr_t)a.tuples, (uintptr_t)a.triples,
                                 (uintptr_t)a.e, (uintptr_t)a.ect, (uintptr_t)a.use_j,
                                 (uintptr_t)a.t_begin, (uintptr_t)a.t_end,
-                                (uintptr_t)opts->ijkabc};
+                                (uintptr_t)opts->ijkabc, (uintptr_t)c->split.stage_cap,
+                                (uintptr_t)split_ctas(c)};
       key.insert(key.end(), std::begin(more), std::end(more));
     }
     // the split operands were cut on st; the capture stream must see them
@@ -241,6 +258,7 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
     ba.queue = b->d_queue + 8 * n;
     ba.workspace = b->d_workspace;
     ba.ws_stride = b->ws_stride;
+    ba.claim = std::max(1, (int)b->tune.tuples_per_claim);
     int64_t launches = 0;
     cudaGraph_t graph = nullptr;
     ATRIP_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
@@ -254,7 +272,8 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
       if (form == ATRIP_FORM_FP64) {
         if (prefix[n] > 0) {
           const int grid = (int)std::min<int64_t>(b->grid, prefix[n]);
-          ATRIP_CUDA_TRY(launch_triples_fp64_batch(ba, b->max_no, grid, b->stream));
+          ATRIP_CUDA_TRY(launch_triples_fp64_batch(ba, b->max_no, b->tune.fp64_min_blocks, grid,
+                                                   b->stream));
           launches += 1;
         }
       } else {
@@ -262,7 +281,7 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
           atrip_gpu_context *c = b->sys[b->order[k]];
           const TriplesArgs &a = b->h_table[k];
           if (a.t_end == a.t_begin) continue;
-          int rc2 = split_enqueue(c->split, c->dt, c->No, c->Nv, c->sm_count, a.tuples,
+          int rc2 = split_enqueue(c->split, c->dt, c->No, c->Nv, split_ctas(c), a.tuples,
                                   a.triples, a.n_triples, a.t_begin, a.t_end, tai_sign,
                                   a.use_j != 0, b->d_queue + 8 * k, a.e, a.ect, b->stream,
                                   &launches);
@@ -319,6 +338,22 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
     r.slices_used = form == ATRIP_FORM_FP64 ? 0 : slices;
     r.kernel_launches = b->graph_launches + prep_launches;
   }
+  return ATRIP_OK;
+}
+
+int atrip_gpu_batch_set_tuning(atrip_gpu_batch *b, const atrip_tuning *t) {
+  clear_error();
+  if (!b || !t) return fail(ATRIP_ERR_ARGUMENT, "null argument");
+  if (t->fp64_ctas_per_sm < 0 || t->tuples_per_claim < 0 || t->tuples_per_claim > 64)
+    return fail(ATRIP_ERR_ARGUMENT, "tuning value out of range");
+  if (t->fp64_min_blocks != 0 && t->fp64_min_blocks != 2)
+    return fail(ATRIP_ERR_ARGUMENT, "fp64_min_blocks must be 0 or 2");
+  ATRIP_CUDA_TRY(cudaSetDevice(b->device));
+  int per_sm = std::max(1, triples_fp64_batch_max_blocks_per_sm(b->max_no, t->fp64_min_blocks));
+  if (t->fp64_ctas_per_sm > 0) per_sm = std::min(per_sm, (int)t->fp64_ctas_per_sm);
+  per_sm = std::min(per_sm, b->max_per_sm);
+  b->tune = *t;
+  b->grid = b->sm_count * per_sm;
   return ATRIP_OK;
 }
 

@@ -323,7 +323,10 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
   if (n > 0) {
     ATRIP_CUDA_TRY(cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned long long) * 4, st));
     if (form == ATRIP_FORM_FP64) {
-      const int per_sm = std::max(1, triples_fp64_max_blocks_per_sm(c->No));
+      const int rows_tile = c->tune.fp64_tile_rows == 32 ? 32 : 64;
+      const int min_blocks = c->tune.fp64_min_blocks == 2 ? 2 : 0;
+      int per_sm = std::max(1, triples_fp64_max_blocks_per_sm(c->No, rows_tile, min_blocks));
+      if (c->tune.fp64_ctas_per_sm > 0) per_sm = std::min(per_sm, (int)c->tune.fp64_ctas_per_sm);
       const int64_t grid = std::min<int64_t>((int64_t)c->sm_count * per_sm, n);
       const size_t ws = (size_t)grid * 2 * (size_t)c->No * c->No * c->No;
       if (ws > c->workspace_doubles) {
@@ -357,10 +360,16 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
       a.e = c->d_e;
       a.ect = c->d_ect;
       a.workspace = c->d_workspace;
+      a.rows_tile = rows_tile;
+      a.claim = std::max(1, (int)c->tune.tuples_per_claim);
+      a.min_blocks = min_blocks;
       ATRIP_CUDA_TRY(launch_triples_fp64(a, (int)grid, st));
       launches += 1;
     } else {
-      int rc = split_run(c->split, c->dt, c->No, c->Nv, c->sm_count, c->d_tuples, c->d_triples,
+      c->split.stage_cap = c->tune.split_stages;
+      const int ctas = c->tune.split_ctas > 0 ? std::min(c->sm_count, (int)c->tune.split_ctas)
+                                              : c->sm_count;
+      int rc = split_run(c->split, c->dt, c->No, c->Nv, ctas, c->d_tuples, c->d_triples,
                          c->n_triples, t_begin, t_end, opts->ijkabc ? -1.0 : 1.0, use_j, slices,
                          c->d_queue, c->d_e, c->d_ect, st, &launches);
       if (rc != ATRIP_OK) return rc;
@@ -390,6 +399,29 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
   out->form_used = form;
   out->slices_used = form == ATRIP_FORM_FP64 ? 0 : slices;
   out->kernel_launches = launches;
+  return ATRIP_OK;
+}
+
+int atrip_gpu_set_tuning(atrip_gpu_context *c, const atrip_tuning *t) {
+  clear_error();
+  if (!c || !t) return fail(ATRIP_ERR_ARGUMENT, "null argument");
+  if (t->fp64_ctas_per_sm < 0 || t->tuples_per_claim < 0 || t->split_ctas < 0)
+    return fail(ATRIP_ERR_ARGUMENT, "negative tuning value");
+  if (t->fp64_tile_rows != 0 && t->fp64_tile_rows != 32 && t->fp64_tile_rows != 64)
+    return fail(ATRIP_ERR_ARGUMENT, "fp64_tile_rows must be 32 or 64");
+  if (t->split_stages != 0 && (t->split_stages < 2 || t->split_stages > 6))
+    return fail(ATRIP_ERR_ARGUMENT, "split_stages must be 2..6");
+  if (t->tuples_per_claim > 64) return fail(ATRIP_ERR_ARGUMENT, "tuples_per_claim must be <= 64");
+  if (t->fp64_min_blocks != 0 && t->fp64_min_blocks != 2)
+    return fail(ATRIP_ERR_ARGUMENT, "fp64_min_blocks must be 0 or 2");
+  c->tune = *t;
+  return ATRIP_OK;
+}
+
+int atrip_gpu_get_tuning(const atrip_gpu_context *c, atrip_tuning *t) {
+  clear_error();
+  if (!c || !t) return fail(ATRIP_ERR_ARGUMENT, "null argument");
+  *t = c->tune;
   return ATRIP_OK;
 }
 

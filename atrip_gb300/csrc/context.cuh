@@ -27,4 +27,5 @@ struct atrip_gpu_context {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   atrip_gb300::SplitState split;
+  atrip_tuning tune = {};
 };

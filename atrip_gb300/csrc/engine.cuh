@@ -50,6 +50,9 @@ struct TriplesArgs {
   int use_j;
   double *e, *ect;          // per-tuple energies, indexed by list position
   double *workspace;        // per-CTA scratch, 2 * No^3 doubles each
+  int rows_tile;            // (p,q) rows per register tile: 32 or 64
+  int claim;                // tuples a CTA takes from the queue at once (>= 1)
+  int min_blocks;           // 2: kernel variant capped at 128 registers, else 0
 };
 
 cudaError_t launch_triples_fp64(const TriplesArgs &a, int grid, cudaStream_t s);
@@ -63,11 +66,15 @@ struct BatchArgs {
   unsigned long long *queue;
   double *workspace;
   int64_t ws_stride;
+  int claim;  // tuples a CTA takes from the queue at once (>= 1)
 };
-cudaError_t launch_triples_fp64_batch(const BatchArgs &b, int max_no, int grid, cudaStream_t s);
+// Batch systems have No <= kBatchMaxNo.
+constexpr int kBatchMaxNo = 32;
+cudaError_t launch_triples_fp64_batch(const BatchArgs &b, int max_no, int min_blocks, int grid,
+                                      cudaStream_t s);
 cudaError_t launch_batch_energy_sum(const BatchArgs &b, double *sums, cudaStream_t s);
-int triples_fp64_max_blocks_per_sm(int No);
-int triples_fp64_batch_max_blocks_per_sm(int max_no);
+int triples_fp64_max_blocks_per_sm(int No, int rows_tile, int min_blocks);
+int triples_fp64_batch_max_blocks_per_sm(int max_no, int min_blocks);
 
 // dst[i0 + n0 (i1 + n1 (i2 + n2 i3))] = src[i0 s0 + i1 s1 + i2 s2 + i3 s3]
 cudaError_t launch_permute4(double *dst, const double *src, const int64_t n[4],

@@ -14,6 +14,7 @@ struct SplitState {
   int slices = 0;
   void *impl = nullptr;
   uint64_t generation = 0;  // bumped whenever device buffers are (re)allocated
+  int stage_cap = 0;        // operand ring depth limit (0 = as many as fit)
 };
 
 void split_invalidate(SplitState &s);

@@ -641,6 +641,7 @@ struct SplitImpl {
   float *wglobal = nullptr;
   size_t wglobal_floats = 0;
   int *d_status = nullptr;
+  int stage_cap = 0;  // operand ring depth limit (0 = as many as fit)
   SplitMaps maps;
 };
 
@@ -881,6 +882,7 @@ int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st
   const size_t avail = kSmemLimit - 1024 - kTailBytes - vbytes;
   int nst = (int)(avail / K::kStageBytes);
   if (nst > kMaxStages) nst = kMaxStages;
+  if (p->stage_cap >= 2 && nst > p->stage_cap) nst = p->stage_cap;
   if (nst < 2) {
     set_error("split form: shared memory too small for No=" + std::to_string(a.No));
     return ATRIP_ERR_UNSUPPORTED;
@@ -976,6 +978,11 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
     return ATRIP_ERR_STATE;
   }
   const size_t need = (size_t)sm_count * 2 * (use_j ? 2 : 1) * 2 * No * No * No;
+  if (need > p->wglobal_floats) {
+    set_error("split form: W buffers prepared for fewer CTAs");
+    return ATRIP_ERR_STATE;
+  }
+  p->stage_cap = s.stage_cap;
   ATRIP_CUDA_TRY(cudaMemsetAsync(p->wglobal, 0, sizeof(float) * need, st));
   ATRIP_CUDA_TRY(cudaMemsetAsync(p->d_status, 0, sizeof(int), st));
   SplitArgs a;

@@ -1,353 +1,63 @@
-// Plain-FP64 form of the per-(a,b,c) triples kernel.
-//
-// One persistent CTA per slot pulls tuples from a device work queue (an
-// atomic cursor over the lexicographic tuple list, src/atrip/Tuples.cxx:
-// 122-134) and, per tuple:
-//   1. builds W = Tijk from six fused contractions.  Each pairs one particle
-//      term of src/atrip/Equations.cxx:709-725 with the hole term that has
-//      the same output layout (:692-708), so one tile loop runs K = Nv + No:
-//        R[(p,q), r] = sum_E A_x[(p,q),E] V_yz[E,r] - sum_L Vh_w[(p,q),L] T_uv[L,r]
-//      and R is added into W at the index permutation of that term (the
-//      reorder<> kernels of src/atrip/Equations.cxx:27-83, fused);
-//   2. forms Zijk = W + singles on the fly (src/atrip/Equations.cxx:387-426);
-//   3. reduces get_energy_{distinct,same} (src/atrip/Equations.cxx:101-238)
-//      over i >= j >= k with a block reduction;
-//   4. for (cT) builds W from the J intermediates and reduces again with the
-//      same Z (src/atrip/Atrip.cxx:928-963).
-// FP64 throughput on this part is ~1 TFLOP/s for DFMA and DMMA alike, so the
-// contraction is a register-tiled DFMA GEMM; the tiles are staged through
-// shared memory with coalesced loads.
-#include "engine.cuh"
+// Plain-FP64 form, one system per launch: the persistent kernel over one
+// context's tuple range (per-tuple work in fp64_tuple.cuh).
+#include "fp64_tuple.cuh"
 
 namespace atrip_gb300 {
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kMT = 64;  // rows (p,q) per tile: 32 row groups x 2
-constexpr int kKC = 32;  // K elements per shared-memory stage
-
-struct Term {
-  const double *Apart;  // Ta_x   rows m, K = Nv
-  const double *Ahole;  // Vht_w  rows m, K = No
-  const double *Bpart;  // Vpt_yz cols r, K = Nv
-  const double *Bhole;  // Tp_uv  No x No block
-  int holeT;            // 0: B[L][r] = T[u,v,L,r]; 1: B[L][r] = T[u,v,r,L]
-  int sp, sq, sr;       // W index = p sp + q sq + r sr
-};
-
-// The six fused terms of tuple (a,b,c); index roles a<->i, b<->j, c<->k.
-__device__ __forceinline__ Term make_term(int t, const TriplesArgs &g, const double *Vht,
-                                          const double *Vpt, int a, int b, int c) {
-  const int64_t No = g.No, Nv = g.Nv, No2 = No * No, No3 = No2 * No;
-  int x, w, y, z, u, v, holeT, sp, sq, sr;
-  switch (t) {
-    case 0: x = a; w = b; y = b; z = c; u = a; v = c; holeT = 0; sp = 1; sq = No; sr = No2; break;
-    case 1: x = a; w = c; y = c; z = b; u = a; v = b; holeT = 0; sp = 1; sq = No2; sr = No; break;
-    case 2: x = c; w = a; y = a; z = b; u = b; v = c; holeT = 1; sp = No2; sq = 1; sr = No; break;
-    case 3: x = c; w = b; y = b; z = a; u = a; v = c; holeT = 1; sp = No2; sq = No; sr = 1; break;
-    case 4: x = b; w = a; y = a; z = c; u = b; v = c; holeT = 0; sp = No; sq = 1; sr = No2; break;
-    default: x = b; w = c; y = c; z = a; u = a; v = b; holeT = 1; sp = No; sq = No2; sr = 1; break;
-  }
-  Term r;
-  r.Apart = g.Ta + (int64_t)x * No2 * Nv;
-  r.Ahole = Vht + (int64_t)w * No3;
-  r.Bpart = Vpt + ((int64_t)y * Nv + z) * No * Nv;
-  r.Bhole = g.Tp + ((int64_t)u * Nv + v) * No2;
-  r.holeT = holeT;
-  r.sp = sp;
-  r.sq = sq;
-  r.sr = sr;
-  return r;
-}
-
-struct Smem {
-  double As[kKC][kMT + 1];
-  double Bs[kKC][64 + 1];
-  double red[kThreads / 32][2];
-  long long tuple_slot;
-};
-
-// W (No^3, in the per-CTA workspace) = sum of the six fused terms.
-template <int NC>
-__device__ void build_w(const TriplesArgs &g, Smem &sm, double *W, const double *Vht,
-                        const double *Vpt, int a, int b, int c) {
-  const int No = g.No, Nv = g.Nv, No2 = No * No;
-  const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;
-  for (int t = 0; t < 6; ++t) {
-    const Term tm = make_term(t, g, Vht, Vpt, a, b, c);
-    for (int m0 = 0; m0 < No2; m0 += kMT) {
-      double acc[2][NC];
-#pragma unroll
-      for (int u = 0; u < 2; ++u)
-#pragma unroll
-        for (int v = 0; v < NC; ++v) acc[u][v] = 0.0;
-      for (int seg = 0; seg < 2; ++seg) {
-        const int K = seg == 0 ? Nv : No;
-        const double *A = seg == 0 ? tm.Apart : tm.Ahole;
-        for (int k0 = 0; k0 < K; k0 += kKC) {
-          for (int idx = tid; idx < kMT * kKC; idx += kThreads) {
-            const int row = idx / kKC, kk = idx % kKC, m = m0 + row, k = k0 + kk;
-            sm.As[kk][row] = (m < No2 && k < K) ? A[(int64_t)m * K + k] : 0.0;
-          }
-          for (int idx = tid; idx < NC * 8 * kKC; idx += kThreads) {
-            const int col = idx / kKC, kk = idx % kKC, k = k0 + kk;
-            double val = 0.0;
-            if (col < No && k < K) {
-              if (seg == 0)
-                val = tm.Bpart[(int64_t)col * Nv + k];
-              else
-                val = -(tm.holeT ? tm.Bhole[k * No + col] : tm.Bhole[col * No + k]);
-            }
-            sm.Bs[kk][col] = val;
-          }
-          __syncthreads();
-#pragma unroll 8
-          for (int kk = 0; kk < kKC; ++kk) {
-            const double a0 = sm.As[kk][ty], a1 = sm.As[kk][ty + 32];
-#pragma unroll
-            for (int v = 0; v < NC; ++v) {
-              const double bv = sm.Bs[kk][tx + 8 * v];
-              acc[0][v] = fma(a0, bv, acc[0][v]);
-              acc[1][v] = fma(a1, bv, acc[1][v]);
-            }
-          }
-          __syncthreads();
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int m = m0 + ty + 32 * u;
-        if (m < No2) {
-          const int p = m % No, q = m / No;
-#pragma unroll
-          for (int v = 0; v < NC; ++v) {
-            const int r = tx + 8 * v;
-            if (r < No) {
-              const int idx = p * tm.sp + q * tm.sq + r * tm.sr;
-              W[idx] = (t == 0 ? 0.0 : W[idx]) + acc[u][v];
-            }
-          }
-        }
-      }
-    }
-    __syncthreads();
-  }
-}
-
-struct SinglesCtx {
-  const double *Vbc, *Vac, *Vab;  // No x No blocks V[x,y,m,n] at [n*No + m]
-  double ta[64], tb[64], tc[64];  // signed t1[a,.], t1[b,.], t1[c,.]
-};
-
-// Zijk at (i,j,k) = W + t1 (x) V, in the order of src/atrip/Equations.cxx:420-422.
-__device__ __forceinline__ double zval(const double *W, const SinglesCtx &s, int No, int i, int j,
-                                       int k) {
-  double z = W[i + No * j + No * No * k];
-  z += s.ta[i] * s.Vbc[j + k * No];
-  z += s.tb[j] * s.Vac[i + k * No];
-  z += s.tc[k] * s.Vab[i + j * No];
-  return z;
-}
-
-// One tuple's energy over i >= j >= k (src/atrip/Equations.cxx:101-238):
-// T from Tb, Z from Wz + singles.  Returns this thread's partial sum.
-__device__ double energy_partial(const TriplesArgs &g, const double *Tb, const double *Wz,
-                                 const SinglesCtx &s, bool distinct, double epsabc) {
-  const int No = g.No;
-  double sum = 0.0;
-  for (int n = threadIdx.x; n < g.n_triples; n += kThreads) {
-    const uint32_t pk = g.triples[n];
-    const int i = pk & 0xff, j = (pk >> 8) & 0xff, k = (pk >> 16) & 0xff;
-    const double facjk = j == k ? 0.5 : 1.0, facij = i == j ? 0.5 : 1.0;
-    const double denominator = epsabc - ((g.epsi[i] + g.epsi[j]) + g.epsi[k]);
-    double value;
-    if (distinct) {
-      const double U = zval(Wz, s, No, i, j, k), V = zval(Wz, s, No, i, k, j),
-                   W = zval(Wz, s, No, j, i, k), X = zval(Wz, s, No, j, k, i),
-                   Y = zval(Wz, s, No, k, i, j), Z = zval(Wz, s, No, k, j, i);
-      const double A = Tb[i + No * j + No * No * k], B = Tb[i + No * k + No * No * j],
-                   C = Tb[j + No * i + No * No * k], D = Tb[j + No * k + No * No * i],
-                   E = Tb[k + No * i + No * No * j], F = Tb[k + No * j + No * No * i];
-      const double UXY = U + (X + Y), VWZ = V + (W + Z), ADE = A + (D + E), BCF = B + (C + F);
-      const double first = A * U + (B * V + (C * W + (D * X + (E * Y + F * Z))));
-      value = 3.0 * first + ((UXY - 2.0 * VWZ) * ADE + (VWZ - 2.0 * UXY) * BCF);
-    } else {
-      const double U = zval(Wz, s, No, i, j, k), V = zval(Wz, s, No, j, k, i),
-                   W = zval(Wz, s, No, k, i, j);
-      const double A = Tb[i + No * j + No * No * k], B = Tb[j + No * k + No * No * i],
-                   C = Tb[k + No * i + No * No * j];
-      value = 3.0 * ((A * U + B * V) + C * W) - (A + (B + C)) * (U + (V + W));
-    }
-    sum += (2.0 * value / denominator) * (facjk * facij);
-  }
-  return sum;
-}
-
-__device__ double block_sum(double v, Smem &sm, int slot) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) sm.red[threadIdx.x >> 5][slot] = v;
-  __syncthreads();
-  double r = 0.0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < kThreads / 32; ++w) r += sm.red[w][slot];
-  return r;  // valid in thread 0
-}
-
-// One tuple t of the system described by g: W (and W_J), energies e[t],
-// ect[t].  All threads of the block take part.
-template <int NC>
-__device__ void process_tuple(const TriplesArgs &g, Smem &sm, SinglesCtx &s, double *Wv,
-                              double *Wj, int64_t t) {
-  const uint32_t pk = g.tuples[t];
-  const int a = pk & 0x3ff, b = (pk >> 10) & 0x3ff, c = (pk >> 20) & 0x3ff;
-  const int No = g.No, Nv = g.Nv, No2 = No * No;
-  if (threadIdx.x < No) {
-    const int i = threadIdx.x;
-    s.ta[i] = g.tai_sign * g.tai[a + i * Nv];
-    s.tb[i] = g.tai_sign * g.tai[b + i * Nv];
-    s.tc[i] = g.tai_sign * g.tai[c + i * Nv];
-  }
-  if (threadIdx.x == 0) {
-    s.Vbc = g.Vhh + ((int64_t)b * Nv + c) * No2;
-    s.Vac = g.Vhh + ((int64_t)a * Nv + c) * No2;
-    s.Vab = g.Vhh + ((int64_t)a * Nv + b) * No2;
-  }
-  build_w<NC>(g, sm, Wv, g.Vht, g.Vpt, a, b, c);
-  // classification of src/atrip/Atrip.cxx:640-642
-  int cls = 0;
-  if (a == b) cls++;
-  if (b == c) cls--;
-  const bool distinct = cls == 0;
-  const double epsabc = g.epsa[a] + g.epsa[b] + g.epsa[c];
-  const double e = block_sum(energy_partial(g, Wv, Wv, s, distinct, epsabc), sm, 0);
-  double ect = e;
-  if (g.use_j) {
-    build_w<NC>(g, sm, Wj, g.Jht, g.Jpt, a, b, c);
-    ect = block_sum(energy_partial(g, Wj, Wv, s, distinct, epsabc), sm, 1);
-  }
-  if (threadIdx.x == 0) {
-    g.e[t] = e;
-    g.ect[t] = ect;
-  }
-  __syncthreads();
-}
-
-template <int NC>
-__global__ void __launch_bounds__(kThreads) triples_fp64_kernel(TriplesArgs g) {
+// A CTA claims g.claim consecutive tuples per queue access.  MINB = 0 leaves
+// the register budget to the compiler; MINB = 2 caps it at 128 registers
+// (two resident CTAs per SM, no spills).
+template <int NC, int RU, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) triples_fp64_kernel(TriplesArgs g) {
   __shared__ Smem sm;
   __shared__ SinglesCtx s;
   const int64_t No3 = (int64_t)g.No * g.No * g.No;
   double *Wv = g.workspace + (int64_t)blockIdx.x * 2 * No3;
   double *Wj = Wv + No3;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const unsigned long long q = atomicAdd(g.queue, 1ull);
-      sm.tuple_slot = (q < (unsigned long long)(g.t_end - g.t_begin)) ? (long long)q : -1;
-    }
-    __syncthreads();
-    const long long slot = sm.tuple_slot;
-    __syncthreads();
-    if (slot < 0) break;
-    process_tuple<NC>(g, sm, s, Wv, Wj, g.t_begin + slot);
-  }
-}
-
-// process_tuple<nc> for the system's own column count nc <= NC, so a small
-// system in a mixed batch does not pay for the largest system's tile width.
-template <int NC>
-__device__ void process_tuple_nc(int nc, const TriplesArgs &g, Smem &sm, SinglesCtx &s,
-                                 double *Wv, double *Wj, int64_t t) {
-  if constexpr (NC > 1) {
-    if (nc < NC) {
-      process_tuple_nc<NC - 1>(nc, g, sm, s, Wv, Wj, t);
-      return;
-    }
-  }
-  process_tuple<NC>(g, sm, s, Wv, Wj, t);
-}
-
-// Many systems in one persistent launch: a single work-queue cursor runs over
-// the concatenated tuple ranges of all systems (prefix[s] .. prefix[s+1]);
-// each tuple is processed with its system's descriptor.
-template <int NC>
-__global__ void __launch_bounds__(kThreads) triples_fp64_batch_kernel(BatchArgs bt) {
-  __shared__ Smem sm;
-  __shared__ SinglesCtx s;
-  __shared__ TriplesArgs sg;
-  __shared__ int sys;
-  double *Wv = bt.workspace + (int64_t)blockIdx.x * bt.ws_stride;
-  double *Wj = Wv + bt.ws_stride / 2;
-  const int64_t total = bt.prefix[bt.n];
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const unsigned long long q = atomicAdd(bt.queue, 1ull);
-      long long slot = -1;
-      int lo = 0;
-      if (q < (unsigned long long)total) {
-        int hi = bt.n;  // prefix[lo] <= q < prefix[hi]
-        while (hi - lo > 1) {
-          const int mid = (lo + hi) / 2;
-          if ((int64_t)q >= bt.prefix[mid]) lo = mid; else hi = mid;
-        }
-        slot = (long long)q - bt.prefix[lo];
-      }
-      sm.tuple_slot = slot;
-      sys = lo;
-    }
-    __syncthreads();
-    const long long slot = sm.tuple_slot;
-    if (slot < 0) break;
-    if (threadIdx.x == 0) sg = bt.systems[sys];
-    __syncthreads();
-    process_tuple_nc<NC>((sg.No + 7) / 8, sg, sm, s, Wv, Wj, sg.t_begin + slot);
-  }
-}
-
-// Per-system compensated sums of e and ect (block s reduces system s, in a
-// fixed order): sums[2 s], sums[2 s + 1].
-__global__ void batch_energy_sum(BatchArgs bt, double *sums) {
-  __shared__ double sh[4][kThreads];
-  const TriplesArgs &g = bt.systems[blockIdx.x];
   const int64_t n = g.t_end - g.t_begin;
-  double s0 = 0, c0 = 0, s1 = 0, c1 = 0;
-  auto neu = [](double &sv, double &cv, double x) {
-    const double t = sv + x;
-    if (fabs(sv) >= fabs(x)) cv += (sv - t) + x; else cv += (x - t) + sv;
-    sv = t;
-  };
-  for (int64_t t = threadIdx.x; t < n; t += kThreads) {
-    neu(s0, c0, g.e[g.t_begin + t]);
-    neu(s1, c1, g.ect[g.t_begin + t]);
-  }
-  sh[0][threadIdx.x] = s0;
-  sh[1][threadIdx.x] = c0;
-  sh[2][threadIdx.x] = s1;
-  sh[3][threadIdx.x] = c1;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a0 = 0, b0 = 0, a1 = 0, b1 = 0;
-    for (int i = 0; i < kThreads; ++i) {
-      neu(a0, b0, sh[0][i]);
-      b0 += sh[1][i];
-      neu(a1, b1, sh[2][i]);
-      b1 += sh[3][i];
+  const int claim = g.claim > 0 ? g.claim : 1;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const unsigned long long q = atomicAdd(g.queue, (unsigned long long)claim);
+      sm.tuple_slot = (q < (unsigned long long)n) ? (long long)q : -1;
     }
-    sums[2 * blockIdx.x] = a0 + b0;
-    sums[2 * blockIdx.x + 1] = a1 + b1;
+    __syncthreads();
+    const long long slot = sm.tuple_slot;
+    __syncthreads();
+    if (slot < 0) break;
+    const int64_t last = slot + claim < n ? slot + claim : n;
+    for (int64_t u = slot; u < last; ++u) process_tuple<NC, RU>(g, sm, s, Wv, Wj, g.t_begin + u);
   }
 }
 
-template <int NC>
-cudaError_t launch_batch_nc(const BatchArgs &b, int grid, cudaStream_t st) {
-  triples_fp64_batch_kernel<NC><<<grid, kThreads, 0, st>>>(b);
+template <int NC, int RU, int MINB>
+cudaError_t launch_v(const TriplesArgs &a, int grid, cudaStream_t s) {
+  triples_fp64_kernel<NC, RU, MINB><<<grid, kThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 template <int NC>
 cudaError_t launch_nc(const TriplesArgs &a, int grid, cudaStream_t s) {
-  triples_fp64_kernel<NC><<<grid, kThreads, 0, s>>>(a);
-  return cudaGetLastError();
+  if (a.rows_tile == 32) return launch_v<NC, 1, 0>(a, grid, s);
+  if (a.min_blocks == 2) return launch_v<NC, 2, 2>(a, grid, s);
+  return launch_v<NC, 2, 0>(a, grid, s);
+}
+
+template <int NC>
+int blocks_nc(int rows_tile, int min_blocks) {
+  int n = 0;
+  cudaError_t e;
+  if (rows_tile == 32)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<NC, 1, 0>,
+                                                      kThreads, 0);
+  else if (min_blocks == 2)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<NC, 2, 2>,
+                                                      kThreads, 0);
+  else
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<NC, 2, 0>,
+                                                      kThreads, 0);
+  return e == cudaSuccess ? n : 0;
 }
 
 }  // namespace
@@ -366,57 +76,18 @@ cudaError_t launch_triples_fp64(const TriplesArgs &a, int grid, cudaStream_t s) 
   }
 }
 
-cudaError_t launch_triples_fp64_batch(const BatchArgs &b, int max_no, int grid, cudaStream_t s) {
-  switch ((max_no + 7) / 8) {
-    case 1: return launch_batch_nc<1>(b, grid, s);
-    case 2: return launch_batch_nc<2>(b, grid, s);
-    case 3: return launch_batch_nc<3>(b, grid, s);
-    case 4: return launch_batch_nc<4>(b, grid, s);
-    case 5: return launch_batch_nc<5>(b, grid, s);
-    case 6: return launch_batch_nc<6>(b, grid, s);
-    case 7: return launch_batch_nc<7>(b, grid, s);
-    case 8: return launch_batch_nc<8>(b, grid, s);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-cudaError_t launch_batch_energy_sum(const BatchArgs &b, double *sums, cudaStream_t s) {
-  batch_energy_sum<<<b.n, kThreads, 0, s>>>(b, sums);
-  return cudaGetLastError();
-}
-
-int triples_fp64_batch_max_blocks_per_sm(int max_no) {
-  int n = 0;
-  cudaError_t e = cudaErrorInvalidValue;
-  switch ((max_no + 7) / 8) {
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<1>, kThreads, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<2>, kThreads, 0); break;
-    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<3>, kThreads, 0); break;
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<4>, kThreads, 0); break;
-    case 5: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<5>, kThreads, 0); break;
-    case 6: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<6>, kThreads, 0); break;
-    case 7: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<7>, kThreads, 0); break;
-    case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_batch_kernel<8>, kThreads, 0); break;
-    default: break;
-  }
-  return e == cudaSuccess ? n : 0;
-}
-
-int triples_fp64_max_blocks_per_sm(int No) {
-  int n = 0;
-  cudaError_t e = cudaErrorInvalidValue;
+int triples_fp64_max_blocks_per_sm(int No, int rows_tile, int min_blocks) {
   switch ((No + 7) / 8) {
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<1>, kThreads, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<2>, kThreads, 0); break;
-    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<3>, kThreads, 0); break;
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<4>, kThreads, 0); break;
-    case 5: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<5>, kThreads, 0); break;
-    case 6: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<6>, kThreads, 0); break;
-    case 7: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<7>, kThreads, 0); break;
-    case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, triples_fp64_kernel<8>, kThreads, 0); break;
-    default: break;
+    case 1: return blocks_nc<1>(rows_tile, min_blocks);
+    case 2: return blocks_nc<2>(rows_tile, min_blocks);
+    case 3: return blocks_nc<3>(rows_tile, min_blocks);
+    case 4: return blocks_nc<4>(rows_tile, min_blocks);
+    case 5: return blocks_nc<5>(rows_tile, min_blocks);
+    case 6: return blocks_nc<6>(rows_tile, min_blocks);
+    case 7: return blocks_nc<7>(rows_tile, min_blocks);
+    case 8: return blocks_nc<8>(rows_tile, min_blocks);
+    default: return 0;
   }
-  return e == cudaSuccess ? n : 0;
 }
 
 }  // namespace atrip_gb300

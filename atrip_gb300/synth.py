@@ -28,7 +28,7 @@ _M1 = np.uint64(0xBF58476D1CE4E5B9)
 _M2 = np.uint64(0x94D049BB133111EB)
 _TENSOR_IDS = {
     "epsi": 1, "epsa": 2, "Tai": 3, "Tabij": 4, "Vabij": 5,
-    "Vijka": 6, "Vabci": 7, "Jijka": 8, "Jabci": 9,
+    "Vijka": 6, "Vabci": 7, "Jijka": 8, "Jabci": 9, "sizes": 10,
 }
 _CHUNK = 1 << 21
 
@@ -141,6 +141,20 @@ def write_bin_dir(d: dict, path: str) -> None:
         if name in d:
             np.asarray(d[name], dtype=np.float64).ravel(order="F").tofile(
                 os.path.join(path, name + ".bin"))
+
+
+def multi_system_sizes(n: int = 96, no_range=(4, 20), nv_range=(30, 200)):
+    """(No, Nv, seed) of the multi-system workload: system s has seed s and
+    No, Nv drawn uniformly (inclusive ranges) from its own counter stream."""
+    out = []
+    for s in range(n):
+        u = _uniform(_key(s, "sizes"), 0, 2)
+        No = no_range[0] + min(int(u[0] * (no_range[1] - no_range[0] + 1)),
+                               no_range[1] - no_range[0])
+        Nv = nv_range[0] + min(int(u[1] * (nv_range[1] - nv_range[0] + 1)),
+                               nv_range[1] - nv_range[0])
+        out.append((No, Nv, s))
+    return out
 
 
 def n_tuples(Nv: int) -> int:

@@ -1,17 +1,30 @@
 """Benchmark of the CCSD(T) triples loop on GB300.
 
-Workload: No=24, Nv=240, seed 0 (the plain-FP64 drop-in configuration of
-the benchmark definition), synthetic inputs with its value distributions.
-A step is one pass of the hot path over one batch of the lexicographic tuple
-list; consecutive steps walk through the list.  The inputs (3.2 GB) are
-larger than L2, so no flush is needed between steps.
+Workloads (synthetic inputs with the benchmark's seeded value distributions):
 
-Metric: FP64-equivalent TFLOP/s of the triples loop, counting atrip's own
-12 No^3 (No + Nv) FLOPs per tuple (src/atrip/Atrip.cxx:578-580); the
-extrapolated time to the full E(T) is reported beside it.
+  no40_nv400  (default) No=40, Nv=400, seed 0: the precision workload, on
+              which the benchmark compares the FP64 and split-BF16 forms
+  no24_nv240  No=24, Nv=240, seed 0 (the plain-FP64 drop-in workload)
+  no56_nv560  No=56, Nv=560, seed 0 (the large single system)
+  no8_nv40    No=8, Nv=40, seed 0 (the reference's own CPU-sized case)
+  batch96     96 systems, No in [4,20], Nv in [30,200], seeds 0..95, one
+              batch (captured graph) per step
 
-  python bench.py [--steps K] [--warmup W] [--form fp64|split_bf16]
-                  [--batch-tuples B] [--impl reference]
+A step is one pass of the hot path over one batch of tuples: for a single
+system a contiguous stretch of the lexicographic tuple list holding about
+1e14 FP64-equivalent FLOPs (the whole list at No=24/Nv=240), consecutive
+steps walking through the list; for batch96 every tuple of every system.
+Inputs (>= 3 GB) are larger than the 129 MB L2, so no flush is needed.
+
+Metric: FP64-equivalent TFLOP/s of the triples loop (atrip's own count,
+12 No^3 (No + Nv) FLOPs per tuple, src/atrip/Atrip.cxx:578-580), with the
+time to the full E(T) beside it.  The default form is the split-BF16 one
+with its slice count and launch parameters chosen by the autotuner; the
+same line carries the FP64 form's throughput on sample windows of the same
+list and the sampled |dE(T)| between the two forms.
+
+  python bench.py [--workload W] [--form split_bf16|fp64] [--steps K]
+                  [--warmup W] [--impl reference]
 """
 from __future__ import annotations
 
@@ -29,14 +42,17 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-NO, NV, SEED = 24, 240, 0
+SEED = 0
+WORKLOADS = {"no8_nv40": (8, 40), "no24_nv240": (24, 240), "no40_nv400": (40, 400),
+             "no56_nv560": (56, 560), "batch96": None}
+DEFAULT_WORKLOAD = "no40_nv400"
+STEP_FLOPS = 1e14        # FP64-equivalent work of one split-form step
+STEP_FLOPS_FP64 = 3e12   # ... of one FP64-form step
 TENSORS = ("epsi", "epsa", "Tai", "Tabij", "Vabij", "Vijka", "Vabci")
 METRIC = "CCSD(T) triples FP64-equivalent TFLOP/s (12 No^3 (No+Nv) per tuple)"
 
 
-def flops_per_tuple(No=None, Nv=None):
-    No = NO if No is None else No
-    Nv = NV if Nv is None else Nv
+def flops_per_tuple(No, Nv):
     return 12.0 * No ** 3 * (No + Nv)
 
 
@@ -83,7 +99,7 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.t.join(timeout=2)
-        sm, smax, reasons = [], [], set()
+        sm, smax, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -92,6 +108,7 @@ class ClockSampler:
             try:
                 sm.append(float(parts[0]))
                 smax.append(float(parts[1]))
+                power.append(float(parts[2]))
             except ValueError:
                 continue
             for nm, val in zip(names, parts[3:7]):
@@ -99,13 +116,27 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
+                "power_w_median": statistics.median(power) if power else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_inputs():
-    from atrip_gb300 import synth
-    return synth.make_inputs(NO, NV, SEED)
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    return json.load(open(path)) if os.path.exists(path) else {}
 
+
+def traffic_per_tuple(kernel: str, workload: str):
+    """DRAM bytes per tuple of `kernel` on `workload` from the committed ncu
+    summary (profiles/traffic.json), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        t = json.load(open(path))
+        return float(t[kernel][workload]["bytes_per_tuple"])
+    except (OSError, KeyError, ValueError, TypeError):
+        return None
+
+
+# ---------------------------------------------------------------- CPU arms
 
 def cpu_baseline(d, seconds=12.0, threads=None):
     """The oracle's DGEMM-route port (numpy's OpenBLAS dgemm, one thread per
@@ -114,21 +145,23 @@ def cpu_baseline(d, seconds=12.0, threads=None):
     import oracle
     threads = threads or os.cpu_count() or 1
     blas = oracle.register_numpy_openblas()
+    No, Nv = d["No"], d["Nv"]
     p = oracle.Problem(d)
     port = oracle.PreparedPort(p)
-    n = int(oracle.n_tuples(NV))
-    probe = min(n, 4 * threads)
+    n = int(oracle.n_tuples(Nv))
+    probe = min(n, 2 * threads)
+    mid = n // 2
     t = time.perf_counter()
-    port.run(0, probe, threads)
+    port.run(mid, min(n, mid + probe), threads)
     dt = max(time.perf_counter() - t, 1e-6)
     sample = int(min(n, max(probe, probe * seconds / dt)))
-    t0 = n // 2  # a middle stretch of the list
+    t0 = max(0, min(mid, n - sample))
     t1 = min(n, t0 + sample)
     t = time.perf_counter()
     port.run(t0, t1, threads)
     dt = time.perf_counter() - t
     port.close()
-    tflops = (t1 - t0) * flops_per_tuple() / dt / 1e12
+    tflops = (t1 - t0) * flops_per_tuple(No, Nv) / dt / 1e12
     return {"value": tflops, "unit": "TFLOP/s", "cores": threads, "kind": "port",
             "sample": f"tuples {t0}..{t1 - 1} of {n} ({t1 - t0} tuples, {dt:.1f} s), DGEMM route "
                       f"with {'OpenBLAS ' + os.path.basename(blas) if blas else 'C loops'}",
@@ -136,95 +169,184 @@ def cpu_baseline(d, seconds=12.0, threads=None):
             "time_to_ET_s_extrapolated": n / ((t1 - t0) / dt)}
 
 
-def run_reference_arm(args):
+def cpu_baseline_batch(ds, seconds=12.0, threads=None):
+    """The port on a bounded sample of the multi-system workload: a stretch
+    of the tuple list of every 12th system, about seconds/8 s each."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    oracle.register_numpy_openblas()
+    flops, secs, parts = 0.0, 0.0, []
+    for d in ds[::12]:
+        No, Nv = d["No"], d["Nv"]
+        n = int(oracle.n_tuples(Nv))
+        port = oracle.PreparedPort(oracle.Problem(d))
+        probe = min(n, 2 * threads)
+        t = time.perf_counter()
+        port.run(0, probe, threads)
+        dt = max(time.perf_counter() - t, 1e-6)
+        m = int(min(n, max(probe, probe * (seconds / 8) / dt)))
+        t0 = (n - m) // 2
+        t = time.perf_counter()
+        port.run(t0, t0 + m, threads)
+        dt = time.perf_counter() - t
+        port.close()
+        flops += m * flops_per_tuple(No, Nv)
+        secs += dt
+        parts.append(f"No={No} Nv={Nv}: {m} tuples")
+    v = flops / secs / 1e12
+    return {"value": v, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+            "sample": "; ".join(parts) + f" ({secs:.1f} s)"}
+
+
+def run_reference_arm(args, workload):
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
-    d = make_inputs()
+    from atrip_gb300 import synth
     import oracle
     threads = os.cpu_count() or 1
     oracle.register_numpy_openblas()
-    p = oracle.Problem(d)
-    port = oracle.PreparedPort(p)
-    n = int(oracle.n_tuples(NV))
-    batch = max(threads, int(args.ref_batch))
-    pos = n // 2
-    for _ in range(args.warmup):
-        port.run(pos, min(n, pos + threads), threads)
-    times = []
-    done = 0
-    for s in range(args.steps):
-        lo = (pos + s * batch) % max(1, n - batch)
-        t = time.perf_counter()
-        port.run(lo, lo + batch, threads)
-        times.append(time.perf_counter() - t)
-        done += batch
-    port.close()
+    if workload == "batch96":
+        sizes = synth.multi_system_sizes(96)[::12]
+        systems = [synth.make_inputs(No, Nv, s) for No, Nv, s in sizes]
+        desc = "every 12th system of the 96-system workload"
+    else:
+        No, Nv = WORKLOADS[workload] if workload in WORKLOADS else (args.no, args.nv)
+        systems = [synth.make_inputs(No, Nv, SEED)]
+        desc = f"No={No} Nv={Nv} seed {SEED}"
+    ports = [(d, oracle.PreparedPort(oracle.Problem(d)), int(oracle.n_tuples(d["Nv"])))
+             for d in systems]
+    times, flops = [], 0.0
+    for step in range(args.warmup + args.steps):
+        t_step, f_step = 0.0, 0.0
+        for d, port, n in ports:
+            fpt = flops_per_tuple(d["No"], d["Nv"])
+            batch = max(threads, int(args.ref_flops / len(ports) / fpt))
+            batch = min(batch, n)
+            lo = ((n // 2) + step * batch) % max(1, n - batch + 1)
+            t = time.perf_counter()
+            port.run(lo, lo + batch, threads)
+            t_step += time.perf_counter() - t
+            f_step += batch * fpt
+        if step >= args.warmup:
+            times.append(t_step)
+            flops += f_step
+    for _, port, _ in ports:
+        port.close()
     total = sum(times)
-    value = done * flops_per_tuple() / total / 1e12
+    value = flops / total / 1e12
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"CCSD(T) triples No={NO} Nv={NV} seed {SEED}",
-                       "tuples_per_step": batch, "l2": "inputs 3.2 GB > L2"},
+            "config": {"workload": workload, "systems": desc,
+                       "flops_per_step": flops / args.steps, "l2": "inputs > L2"},
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} steps of {batch} tuples from tuple {pos}"},
+                             "sample": f"{args.steps} steps of ~{args.ref_flops:.0e} FLOPs, "
+                                       f"stretches from the middle of the tuple list ({desc})"},
             "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0},
-            "time_to_ET_s_extrapolated": n * total / done}
+                    "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
 
 
-def main():
-    global NO, NV
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--form", default="fp64", choices=["fp64", "split_bf16"])
-    ap.add_argument("--slices", type=int, default=0)
-    ap.add_argument("--batch-tuples", type=int, default=0,
-                    help="tuples per step (default: whole list for split, 1%% for fp64)")
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--ref-batch", type=int, default=2048)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no", type=int, default=NO, help="override No (profiling captures)")
-    ap.add_argument("--nv", type=int, default=NV, help="override Nv (profiling captures)")
-    args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
-    NO, NV = args.no, args.nv
-    if args.impl == "reference":
-        return run_reference_arm(args)
+# ---------------------------------------------------------------- GPU arm
 
-    import torch
-    from atrip_gb300 import capi
-
-    world, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    d = make_inputs()
-    n = capi.n_tuples(NV)
-    batch = args.batch_tuples or (n if args.form != "fp64" else max(1, n // 100))
-    batch = min(batch, n)
-    # weak scaling: rank r walks its own stretch of the tuple list
-    origin = (rank * batch) % n
-
-    ctx = capi.Context(NO, NV, local)
-    for name in TENSORS:
+def _upload_all(ctx, d, names=TENSORS):
+    for name in names:
         ctx.upload(name, d[name])
+
+
+def _pinned(d):
+    import torch
+    out, nbytes = {}, 0
+    for name in TENSORS:
+        flat = np.ascontiguousarray(np.asarray(d[name]).ravel(order="F"))
+        t = torch.from_numpy(flat).pin_memory()
+        out[name] = t
+        nbytes += t.numel() * 8
+    return out, nbytes
+
+
+def _timed(steps, stream, fn):
+    """Run fn(s) for s < steps between CUDA events on stream, with the
+    clocks sampled meanwhile.  Returns (ms, results, clocks)."""
+    import torch
+    clocks = ClockSampler(torch.cuda.current_device())
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    res = [fn(s) for s in range(steps)]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    return ms, res, clocks.stop()
+
+
+def _max_over_ranks(world, ms, count):
+    if world <= 1:
+        return ms, count
+    import torch
+    t = torch.tensor([ms], device="cuda")
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    c = torch.tensor([float(count)], device="cuda")
+    torch.distributed.all_reduce(c)
+    return float(t.item()), c.item()
+
+
+def _roofline(form, slices, flops_per_launch, launch_ms, peaks, live_fp64, traffic):
+    if form == "fp64":
+        achieved = flops_per_launch / (launch_ms * 1e-3) / 1e12
+        peak = live_fp64
+        src = "measured FP64 DFMA/DMMA peak (live, atrip_gpu_measure_peaks)"
+        kernel = "triples_fp64_kernel"
+    else:
+        products = slices * (slices + 1) // 2
+        achieved = flops_per_launch * products / (launch_ms * 1e-3) / 1e12
+        peak = peaks.get("bf16_tflops", 1900.0)
+        src = ("of measured BF16 dense peak (bf16_tflops, burst)" if "bf16_tflops" in peaks
+               else "of fallback BF16 peak")
+        kernel = "triples_split_kernel"
+    return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_source": src, "kernel": kernel,
+            "algorithmic": ("FP64-equivalent FLOPs per launch" if form == "fp64" else
+                            f"BF16 MMA FLOPs per launch = FP64-equivalent x S(S+1)/2 = "
+                            f"{slices * (slices + 1) // 2} digit products (S={slices}), "
+                            "unpadded")}
+
+
+def run_single(args, workload, world, rank, local):
+    import torch
+    from atrip_gb300 import autotune, capi, synth
+
+    No, Nv = WORKLOADS[workload] if workload in WORKLOADS else (args.no, args.nv)
+    fpt = flops_per_tuple(No, Nv)
+    t_gen = time.perf_counter()
+    d = synth.make_inputs(No, Nv, SEED)
+    t_gen = time.perf_counter() - t_gen
+    n = capi.n_tuples(Nv)
+    form = args.form
+    batch = args.batch_tuples or max(1, int((STEP_FLOPS if form != "fp64" else STEP_FLOPS_FP64)
+                                            / fpt))
+    batch = min(batch, n)
+    origin = (rank * batch) % n  # weak scaling: rank r walks its own stretch
+
+    ctx = capi.Context(No, Nv, local)
+    _upload_all(ctx, d)
     stream = torch.cuda.Stream()
+    if args.no_tune:
+        tune = {"tuning": ctx.get_tuning(), "slices": args.slices or 3}
+    else:
+        tune = autotune.tune(ctx, form, tol_eh=args.tol_eh, use_cache=not args.retune,
+                             slices=args.slices)
+    slices = tune["slices"] if form != "fp64" else 0
 
     def step(s):
         lo = (origin + s * batch) % n
         hi = min(n, lo + batch)
-        return ctx.run(form=args.form, slices=args.slices, first_iteration=lo,
+        return ctx.run(form=form, slices=slices, use_j=False, first_iteration=lo,
                        max_iterations=hi - 1, stream=stream.cuda_stream)
 
     for s in range(args.warmup):
@@ -232,103 +354,235 @@ def main():
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    launches, tuples, kernel_ms = 0, 0, []
-    form_used = None
-    for s in range(args.steps):
-        r = step(s)
-        launches += r.kernel_launches
-        tuples += r.tuples_done
-        kernel_ms.append(r.device_ms)
-        form_used = r.form_used
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
-    clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        tt = torch.tensor([float(tuples)], device="cuda")
-        torch.distributed.all_reduce(tt)
-        tuples_all = int(tt.item())
-    else:
-        tuples_all = tuples
-    value = tuples_all * flops_per_tuple() / (ms * 1e-3) / 1e12
+    ms, res, clk = _timed(args.steps, stream, step)
+    tuples = sum(r.tuples_done for r in res)
+    launches = sum(r.kernel_launches for r in res)
+    ms, tuples_all = _max_over_ranks(world, ms, tuples)
+    value = tuples_all * fpt / (ms * 1e-3) / 1e12
+    time_to_et = n * fpt / (value * 1e12)  # whole list at the whole job's rate
+
+    # ---- FP64 form on sample windows of the same list (and the error estimate)
+    compare = None
+    if form != "fp64" and not args.no_compare:
+        m = 16
+        wins = autotune.windows(n, m, autotune.window_size(No, Nv, m, args.compare_flops))
+        tuned = ctx.get_tuning()
+        fp64_tune = autotune.tune(ctx, "fp64", use_cache=not args.retune)["tuning"]
+        ms64, e64 = autotune.run_windows(ctx, wins, "fp64")
+        ctx.set_tuning(**tuned)
+        ms_s, es = autotune.run_windows(ctx, wins, "split_bf16", slices)
+        est = autotune.error_estimate(n, e64, es)
+        n_s = est["sample_tuples"]
+        fp64_tflops = n_s * fpt / (ms64 * 1e-3) / 1e12
+        compare = {"fp64_tflops": fp64_tflops,
+                   "fp64_time_to_ET_s": n * fpt / (fp64_tflops * 1e12),
+                   "fp64_tuning": fp64_tune,
+                   "speedup_split_vs_fp64": (n * fpt / (fp64_tflops * 1e12)) / time_to_et,
+                   "windows": f"{len(wins)} windows x {wins[0][1] - wins[0][0]} tuples",
+                   "accuracy": {k: est[k] for k in ("E_est", "dE_est", "dE_stderr", "rel",
+                                                    "twin_scale_log2", "twin_E", "twin_dE",
+                                                    "twin_dE_bound", "max_tuple_rel",
+                                                    "sample_tuples")},
+                   "tolerance_eh": args.tol_eh}
 
     # ---- end to end through the C ABI with host (pinned) buffers
-    pinned = {}
-    h2d = 0
-    for name in TENSORS:
-        flat = np.ascontiguousarray(np.asarray(d[name]).ravel(order="F"))
-        t = torch.from_numpy(flat).pin_memory()
-        pinned[name] = t
-        h2d += t.numel() * 8
+    pinned, h2d = _pinned(d)
     e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 3))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2e_tuples = 0
     for s in range(e2e_steps):
-        with capi.Context(NO, NV, local) as c2:
+        with capi.Context(No, Nv, local) as c2:
+            c2.set_tuning(**ctx.get_tuning())
             for name in TENSORS:
                 c2.upload_ptr(name, pinned[name].data_ptr(), pinned[name].numel(), False)
             lo = (origin + s * batch) % n
             hi = min(n, lo + batch)
-            r = c2.run(form=args.form, slices=args.slices, first_iteration=lo,
+            r = c2.run(form=form, slices=slices, use_j=False, first_iteration=lo,
                        max_iterations=hi - 1)
             e2e_tuples += r.tuples_done
     e2e_s = time.perf_counter() - t0
-    e2e_value = (e2e_tuples * flops_per_tuple() / e2e_s / 1e12 * (world if world > 1 else 1)
-                 if e2e_steps else None)
+    e2e_value = (e2e_tuples * fpt / e2e_s / 1e12 * max(world, 1)) if e2e_steps else None
 
     if rank != 0:
+        ctx.close()
         return 0
-    # ---- roofline of the dominant kernel
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
-        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    if form_used == capi.FORM_FP64:
-        fp64_peak, _ = capi.measure_peaks(local)
-        peak, peak_note = fp64_peak, "measured FP64 peak (max of DFMA and DMMA loops, live)"
-        achieved = batch * flops_per_tuple() / (statistics.median(kernel_ms) * 1e-3) / 1e12
-        dtype = "f64"
-    else:
-        peak = peaks.get("bf16_tflops", 1900.0)
-        peak_note = "of measured BF16 dense peak (MEASURED_PEAKS.json bf16_tflops)"
-        s_used = args.slices or 3
-        products = s_used * (s_used + 1) // 2
-        achieved = (batch * flops_per_tuple() * products /
-                    (statistics.median(kernel_ms) * 1e-3) / 1e12)
-        dtype = "bf16x%d->f64" % s_used
+    peaks = load_peaks()
+    live_fp64 = capi.measure_peaks(local)[0] if form == "fp64" else None
+    kernel_ms = statistics.median(r.device_ms for r in res)
+    kname = "triples_fp64_kernel" if form == "fp64" else "triples_split_kernel"
+    tpt = traffic_per_tuple(kname, workload)
+    roof = _roofline(form, slices, batch * fpt, kernel_ms, peaks, live_fp64,
+                     tpt * batch if tpt is not None else None)
     cpu = None if args.no_cpu_baseline else cpu_baseline(d, args.cpu_seconds)
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if form == "fp64" else f"bf16x{slices}->f64",
         "data": "synthetic (seeded, benchmark value distributions)",
-        "config": {"workload": f"CCSD(T) triples No={NO} Nv={NV} seed {SEED}",
-                   "form": args.form, "tuples_per_step": batch, "n_tuples": n,
-                   "l2": "no flush: inputs 3.2 GB > 129 MB L2",
-                   "time_to_ET_s": n * (ms / 1e3) / max(tuples_all, 1)},
-        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_note,
-                     "kernel": "triples_fp64_kernel" if form_used == capi.FORM_FP64
-                     else "triples_split_kernel"},
+        "config": {"workload": f"CCSD(T) triples No={No} Nv={Nv} seed {SEED}", "name": workload,
+                   "form": form, "slices": slices, "tuning": tune["tuning"],
+                   "tuples_per_step": batch, "n_tuples": n,
+                   "l2": "no flush: inputs > 129 MB L2",
+                   "time_to_ET_s": time_to_et, "input_gen_s": t_gen},
+        "compare_fp64": compare,
+        "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": 16,
                 "note": "per step: context create, pinned H2D + re-layout of all inputs, "
-                        "tuple batch, energies D2H"},
+                        "split operands cut (split form), the step's tuples, energies D2H"},
         "clocks": clk,
         "gpu_launches": launches,
     }
     print(json.dumps(line))
     ctx.close()
     return 0
+
+
+def run_batch96(args, world, rank, local):
+    import torch
+    from atrip_gb300 import autotune, capi, synth
+
+    sizes = synth.multi_system_sizes(96)
+    t_gen = time.perf_counter()
+    ds = [synth.make_inputs(No, Nv, s) for No, Nv, s in sizes]
+    t_gen = time.perf_counter() - t_gen
+    total_flops = sum(capi.n_tuples(Nv) * flops_per_tuple(No, Nv) for No, Nv, _ in sizes)
+    total_tuples = sum(capi.n_tuples(Nv) for _, Nv, _ in sizes)
+    ctxs = []
+    for d in ds:
+        c = capi.Context(d["No"], d["Nv"], local)
+        _upload_all(c, d)
+        ctxs.append(c)
+    form = args.form
+    slices = args.slices or 3
+    tiles = autotune.tune_batch_tiles(ctxs)
+    b = capi.Batch(ctxs)
+    btune = autotune.tune_batch(b)
+    stream = torch.cuda.Stream()
+
+    def step(s):
+        return b.run(form=form, slices=slices, use_j=False, stream=stream.cuda_stream)
+
+    for s in range(args.warmup):
+        step(s)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms, res, clk = _timed(args.steps, stream, step)
+    launches = sum(r[0].kernel_launches for r in res)
+    ms, _ = _max_over_ranks(world, ms, 0)
+    value = total_flops * args.steps * max(world, 1) / (ms * 1e-3) / 1e12
+
+    # FP64 form and accuracy on the first W tuples of every system
+    W = 512
+    r64 = b.run(form="fp64", use_j=False, max_iterations=W - 1)
+    e64 = [c.tuple_energies(0, r.tuples_done)[0].copy() for c, r in zip(ctxs, r64)]
+    rs = b.run(form="split_bf16", slices=slices, use_j=False, max_iterations=W - 1)
+    es = [c.tuple_energies(0, r.tuples_done)[0].copy() for c, r in zip(ctxs, rs)]
+    wflops = sum(min(W, capi.n_tuples(Nv)) * flops_per_tuple(No, Nv) for No, Nv, _ in sizes)
+    fp64_tflops = wflops / (r64[0].device_ms * 1e-3) / 1e12
+    rel = [float(np.max(np.abs(x - y)) / max(float(np.max(np.abs(y))), 1e-300))
+           for x, y in zip(es, e64)]
+    compare = {"fp64_tflops": fp64_tflops, "fp64_time_to_ET_s": total_flops / fp64_tflops / 1e12,
+               "speedup_split_vs_fp64": (total_flops / fp64_tflops / 1e12) / (ms / args.steps / 1e3),
+               "windows": f"first {W} tuples of every system",
+               "accuracy": {"max_tuple_rel": max(rel)}}
+
+    pinned = [_pinned(d) for d in ds]
+    h2d = sum(p[1] for p in pinned)
+    e2e_steps = 0 if args.no_e2e else 1
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        cs = []
+        for d, (pin, _) in zip(ds, pinned):
+            c2 = capi.Context(d["No"], d["Nv"], local)
+            for name in TENSORS:
+                c2.upload_ptr(name, pin[name].data_ptr(), pin[name].numel(), False)
+            cs.append(c2)
+        with capi.Batch(cs) as b2:
+            b2.run(form=form, slices=slices, use_j=False)
+        for c2 in cs:
+            c2.close()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = total_flops * e2e_steps / e2e_s / 1e12 if e2e_steps else None
+
+    if rank != 0:
+        return 0
+    peaks = load_peaks()
+    kernel_ms = statistics.median(r[0].device_ms for r in res)
+    roof = _roofline(form, slices, total_flops, kernel_ms, peaks,
+                     capi.measure_peaks(local)[0] if form == "fp64" else None, None)
+    roof["note"] = "whole batch graph (all systems' launches and the energy reduction)"
+    cpu = None if args.no_cpu_baseline else cpu_baseline_batch(ds, args.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if form == "fp64" else f"bf16x{slices}->f64",
+        "data": "synthetic (seeded, benchmark value distributions)",
+        "config": {"workload": "96 CCSD(T) triples systems, No in [4,20], Nv in [30,200], "
+                               "seeds 0..95", "name": "batch96", "form": form, "slices": slices,
+                   "tuples_per_step": total_tuples, "flops_per_step": total_flops,
+                   "fp64_row_tiles": {"32": tiles.count(32), "64": tiles.count(64)},
+                   "batch_tuning": btune["tuning"], "l2": "no flush: inputs > 129 MB L2",
+                   "time_to_ET_s": ms / args.steps / 1e3, "input_gen_s": t_gen},
+        "compare_fp64": compare,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": 16 * len(ds),
+                "note": "per step: 96 contexts created, pinned H2D + re-layout, batch run"},
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line))
+    b.close()
+    for c in ctxs:
+        c.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
+                    choices=sorted(WORKLOADS) + ["custom"])
+    ap.add_argument("--form", default="split_bf16", choices=["fp64", "split_bf16"])
+    ap.add_argument("--slices", type=int, default=0, help="0: chosen by the autotuner")
+    ap.add_argument("--tol-eh", type=float, default=1e-8)
+    ap.add_argument("--retune", action="store_true", help="ignore the tuning cache")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="built-in launch parameters, --slices or 3 slices (profiling runs)")
+    ap.add_argument("--batch-tuples", type=int, default=0)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ref-flops", type=float, default=1e12)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--compare-flops", type=float, default=4e12)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no", type=int, default=24, help="No of --workload custom")
+    ap.add_argument("--nv", type=int, default=240, help="Nv of --workload custom")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference_arm(args, args.workload)
+
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    if args.workload == "batch96":
+        return run_batch96(args, world, rank, local)
+    return run_single(args, args.workload, world, rank, local)
 
 
 if __name__ == "__main__":

@@ -133,6 +133,24 @@ int atrip_gpu_release(atrip_gpu_context *ctx, int32_t tensor);
  * (src/atrip/Equations.cxx:101-238, 387-426, 455-728). Blocks until done. */
 int atrip_gpu_run(atrip_gpu_context *ctx, const atrip_run_options *opts, atrip_result *out);
 
+/* Launch parameters chosen by the autotuner (atrip_gb300/autotune.py);
+ * a zero field keeps the built-in choice.  No counterpart in the reference,
+ * whose only tuning knob for this loop is the tuple distribution.          */
+typedef struct {
+  int32_t fp64_ctas_per_sm; /* FP64 form: resident CTAs per SM (0 = occupancy max) */
+  int32_t fp64_tile_rows;   /* FP64 form: (p,q) rows per register tile, 32 or 64    */
+  int32_t tuples_per_claim; /* FP64 form: tuples a CTA takes per queue access       */
+  int32_t split_stages;     /* split form: operand ring depth, 2..6 (0 = all fit)   */
+  int32_t split_ctas;       /* split form: persistent CTAs, <= SMs (0 = one per SM) */
+  int32_t fp64_min_blocks;  /* FP64 form: 2 = kernel built for 2 CTAs/SM (<= 128   */
+                            /* registers), 0 = register budget left to the compiler */
+  int32_t reserved[2];
+} atrip_tuning;
+
+/* Set / read the context's launch parameters (kept until changed). */
+int atrip_gpu_set_tuning(atrip_gpu_context *ctx, const atrip_tuning *tuning);
+int atrip_gpu_get_tuning(const atrip_gpu_context *ctx, atrip_tuning *tuning);
+
 /* Per-tuple energies of the last run, tuple-list positions t0 .. t0+n-1
  * (the sign atrip accumulates before its final negation). ect may be NULL. */
 int atrip_gpu_tuple_energies(atrip_gpu_context *ctx, int64_t t0, int64_t n, double *e,
@@ -166,8 +184,9 @@ int atrip_gpu_measure_peaks(int32_t device, double *fp64_tflops, double *fp32_tf
  * system.  Either sequence is captured into a CUDA graph on the first run
  * and replayed by later runs with the same form, slice count and range.
  *
- * atrip_gpu_batch_create: systems[0..n-1] are contexts on one device; the
- * batch keeps the pointers (destroy the batch before any of them).
+ * atrip_gpu_batch_create: systems[0..n-1] are contexts on one device with
+ * No <= 32; the batch keeps the pointers (destroy the batch before any of
+ * them).
  * atrip_gpu_batch_run: opts as for atrip_gpu_run, applied to every system
  * (start_energy must be 0); results[s] belongs to systems[s], its
  * device_ms and kernel_launches cover the whole batch.  Afterwards
@@ -181,6 +200,10 @@ int atrip_gpu_batch_run(atrip_gpu_batch *batch, const atrip_run_options *opts,
                         atrip_result *results);
 int atrip_gpu_batch_destroy(atrip_gpu_batch *batch);
 int atrip_gpu_batch_plan(const int32_t *no, const int32_t *nv, int32_t n, int32_t *order);
+/* FP64 launch parameters of the batch kernel (fp64_ctas_per_sm,
+ * fp64_min_blocks, tuples_per_claim); the row tile is each context's own
+ * fp64_tile_rows and the split fields are each context's own.             */
+int atrip_gpu_batch_set_tuning(atrip_gpu_batch *batch, const atrip_tuning *tuning);
 
 /* ---------------------------------------------------------------------
  * No-allocation variant (no counterpart in the reference).

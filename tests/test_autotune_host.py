@@ -1,0 +1,45 @@
+"""Host logic of the autotuner (no GPU): sample windows and the sampled
+error estimate that picks the split form's slice count."""
+import math
+
+import numpy as np
+
+from atrip_gb300 import autotune
+
+
+def test_windows_cover_the_list_evenly():
+    for n, m, w in [(100, 4, 10), (11440, 16, 37), (5, 8, 2), (7, 3, 100)]:
+        wins = autotune.windows(n, m, w)
+        assert len(wins) <= m
+        for lo, hi in wins:
+            assert 0 <= lo < hi <= n
+        for (l0, h0), (l1, h1) in zip(wins, wins[1:]):
+            assert h0 <= l1  # disjoint, ordered
+    wins = autotune.windows(1000, 10, 10)
+    assert [lo for lo, _ in wins][0] < 100 and wins[-1][1] > 900
+
+
+def test_window_size_tracks_flops():
+    w = autotune.window_size(24, 240, 8, 1e12)
+    fpt = 12 * 24 ** 3 * (24 + 240)
+    assert abs(w * 8 * fpt - 1e12) <= 8 * fpt
+    assert autotune.window_size(64, 1000, 8, 1.0) == 1
+
+
+def test_error_estimate_extrapolates_and_scales_the_twin():
+    rng = np.random.default_rng(0)
+    ref = [rng.normal(1e-3, 1e-4, 50) for _ in range(8)]
+    delta = 1e-12
+    test = [r + delta for r in ref]
+    n = 10_000
+    est = autotune.error_estimate(n, ref, test)
+    assert math.isclose(est["dE_est"], -n * delta, rel_tol=1e-6)
+    assert math.isclose(est["E_est"], -n / 400 * sum(float(r.sum()) for r in ref), rel_tol=1e-12)
+    assert est["dE_stderr"] < 1e-3 * abs(est["dE_est"])  # constant shift: no spread
+    k = est["twin_scale_log2"]
+    assert 0.1 / 16 <= abs(est["twin_E"]) <= 0.1 * 16
+    assert math.isclose(est["twin_dE"], abs(est["dE_est"]) * 2.0 ** (4 * k))
+    assert est["sample_tuples"] == 400
+    # ijkabc keeps atrip's accumulated sign
+    est2 = autotune.error_estimate(n, ref, test, ijkabc=True)
+    assert math.isclose(est2["dE_est"], n * delta, rel_tol=1e-6)
