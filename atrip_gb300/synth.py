@@ -31,6 +31,7 @@ _TENSOR_IDS = {
     "Vijka": 6, "Vabci": 7, "Jijka": 8, "Jabci": 9, "sizes": 10,
 }
 _CHUNK = 1 << 21
+_IMAG_SEED_OFFSET = 1 << 40  # imaginary parts of complex inputs: seed + this
 
 
 def _mix(z: np.ndarray) -> np.ndarray:
@@ -99,13 +100,30 @@ def _pair_symmetrise(x: np.ndarray) -> np.ndarray:
 
 
 def make_inputs(No: int, Nv: int, seed: int = 0, with_j: bool = False,
-                scale: float = 1.0) -> dict:
+                scale: float = 1.0, field: str = "real", eps_imag: float = 0.0) -> dict:
     """All atrip inputs as Fortran-ordered FP64 arrays.
 
     ``scale`` multiplies t1, t2 and every integral tensor; a power of two
     keeps the relative structure bit-for-bit and scales E(T) by scale**4
     (used for the small-magnitude twin of a workload).
+
+    ``field="complex"`` gives complex128 arrays (atrip's run<Complex>): the
+    real parts are the real workload's arrays, the imaginary parts come from
+    their own streams with the same distributions (and the same pair
+    symmetry for t2 and V_pphh); orbital energies get an imaginary part
+    ~ N(0, eps_imag) (0: real orbital energies, as in CCSD(T)).
     """
+    if field == "complex":
+        re = make_inputs(No, Nv, seed, with_j, scale)
+        im = make_inputs(No, Nv, seed + _IMAG_SEED_OFFSET, with_j, scale)
+        d = {"No": No, "Nv": Nv, "seed": seed}
+        for n in ("Tai", "Tabij", "Vabij", "Vijka", "Vabci", "Jijka", "Jabci"):
+            if n in re:
+                d[n] = np.asfortranarray(re[n] + 1j * im[n])
+        for n, m in (("epsi", No), ("epsa", Nv)):
+            d[n] = re[n] + 1j * (eps_imag * _normal_flat(_key(seed + 2 * _IMAG_SEED_OFFSET, n), m, 1.0) if eps_imag
+                                 else np.zeros(m))
+        return d
     key = lambda name: _key(seed, name)  # noqa: E731
     d = {
         "No": No, "Nv": Nv, "seed": seed,
@@ -135,11 +153,13 @@ def write_bin_dir(d: dict, path: str) -> None:
     import os
     os.makedirs(path, exist_ok=True)
     has_j = int("Jijka" in d)
+    cplx = int(np.iscomplexobj(d["Tabij"]))
     with open(os.path.join(path, "meta.txt"), "w") as f:
-        f.write(f"{d['No']} {d['Nv']} {has_j}\n")
+        f.write(f"{d['No']} {d['Nv']} {has_j} {cplx}\n")
+    dtype = np.complex128 if cplx else np.float64
     for name in ("epsi", "epsa", "Tai", "Tabij", "Vabij", "Vijka", "Vabci", "Jijka", "Jabci"):
         if name in d:
-            np.asarray(d[name], dtype=np.float64).ravel(order="F").tofile(
+            np.asarray(d[name], dtype=dtype).ravel(order="F").tofile(
                 os.path.join(path, name + ".bin"))
 
 

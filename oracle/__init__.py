@@ -31,10 +31,12 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the C restatement (gcc, seconds)."""
-    src = os.path.join(HERE, "triples_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("triples_oracle.c", "triples_oracle_z.c")]
+    stale = not os.path.exists(LIB_PATH) or any(
+        os.path.getmtime(LIB_PATH) < os.path.getmtime(s) for s in srcs)
+    if force or stale:
         tmp = LIB_PATH + f".tmp{os.getpid()}"
-        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-o", tmp, src,
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-o", tmp, *srcs,
                                "-lpthread", "-ldl", "-lm"])
         os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -87,6 +89,15 @@ def _load():
                                         ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.c_void_p]
         lib.oracle_port_free.argtypes = [ctypes.c_void_p]
+        lib.oracle_z_tuple_energies.restype = ctypes.c_int
+        lib.oracle_z_tuple_energies.argtypes = [ctypes.POINTER(_Inputs), ctypes.c_void_p,
+                                                ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                ctypes.c_void_p]
+        lib.oracle_z_tuple_arrays.restype = ctypes.c_int
+        lib.oracle_z_tuple_arrays.argtypes = [ctypes.POINTER(_Inputs), ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_void_p, ctypes.c_void_p]
         _lib = lib
     return _lib
 
@@ -96,15 +107,20 @@ def _ptr(a):
 
 
 class Problem:
-    """Keeps the column-major arrays alive and hands them to the C oracle."""
+    """Keeps the column-major arrays alive and hands them to the C oracle.
+    Complex inputs (any complex array) make a complex problem: every array
+    is then held as complex128, i.e. interleaved (re, im) FP64."""
 
     def __init__(self, d: dict):
         self.No, self.Nv = int(d["No"]), int(d["Nv"])
         self.arrays = {}
-        for n in ("epsi", "epsa", "Tai", "Tabij", "Vabij", "Vijka", "Vabci", "Jijka", "Jabci"):
+        names = ("epsi", "epsa", "Tai", "Tabij", "Vabij", "Vijka", "Vabci", "Jijka", "Jabci")
+        self.complex = any(d.get(n) is not None and np.iscomplexobj(d[n]) for n in names)
+        dtype = np.complex128 if self.complex else np.float64
+        for n in names:
             a = d.get(n)
             if a is not None:
-                a = np.asfortranarray(a, dtype=np.float64)
+                a = np.asfortranarray(a, dtype=dtype)
             self.arrays[n] = a
         self.c = _Inputs(self.No, self.Nv, *[_ptr(self.arrays[n]) for n in
                                              ("epsi", "epsa", "Tai", "Tabij", "Vabij", "Vijka",
@@ -128,11 +144,18 @@ def tuple_list(Nv: int) -> np.ndarray:
 
 def tuple_energies(p: Problem, t0: int = 0, t1: int | None = None, ijkabc: bool = False,
                    use_j: bool = True, route: str = "naive", threads: int = 1):
-    """Per-tuple (e, e_ct) for lexicographic tuples t0..t1-1."""
+    """Per-tuple (e, e_ct) for lexicographic tuples t0..t1-1 (a complex
+    problem always takes the complex restatement)."""
     n = n_tuples(p.Nv)
     t1 = n if t1 is None else t1
     e = np.zeros(max(t1 - t0, 1))
     ect = np.zeros(max(t1 - t0, 1))
+    if p.complex:
+        lst = np.ascontiguousarray(tuple_list(p.Nv))
+        _load().oracle_z_tuple_energies(ctypes.byref(p.c), lst.ctypes.data, t0, t1, int(ijkabc),
+                                        int(use_j), max(1, threads), e.ctypes.data,
+                                        ect.ctypes.data)
+        return e[:t1 - t0], ect[:t1 - t0]
     rc = _load().oracle_tuple_energies(ctypes.byref(p.c), t0, t1, int(ijkabc), int(use_j),
                                        {"naive": 0, "port": 1}[route], threads,
                                        e.ctypes.data, ect.ctypes.data)
@@ -188,6 +211,12 @@ class PreparedPort:
 
 def tuple_arrays(p: Problem, a: int, b: int, c: int, ijkabc: bool = False):
     No = p.No
+    if p.complex:
+        T = np.zeros(No ** 3, dtype=np.complex128)
+        Z = np.zeros(No ** 3, dtype=np.complex128)
+        _load().oracle_z_tuple_arrays(ctypes.byref(p.c), a, b, c, int(ijkabc), T.ctypes.data,
+                                      Z.ctypes.data)
+        return T, Z
     T = np.zeros(No ** 3)
     Z = np.zeros(No ** 3)
     _load().oracle_tuple_arrays(ctypes.byref(p.c), a, b, c, int(ijkabc), T.ctypes.data, Z.ctypes.data)

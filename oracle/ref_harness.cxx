@@ -1,10 +1,12 @@
 /* Driver that runs the UNMODIFIED atrip reference sources as a one-rank CPU
  * oracle (test infrastructure only; never linked into the product).
  *
- * Inputs: a directory holding meta.txt ("No Nv hasJ") and column-major FP64
- * .bin files epsi, epsa, Tai, Tabij, Vabij, Vijka, Vabci [, Jijka, Jabci] --
- * exactly the arrays CTF's read_all would return for atrip's input tensors
- * (src/atrip/Atrip.hpp:68-107).
+ * Inputs: a directory holding meta.txt ("No Nv hasJ [complex]") and
+ * column-major .bin files epsi, epsa, Tai, Tabij, Vabij, Vijka, Vabci
+ * [, Jijka, Jabci] -- exactly the arrays CTF's read_all would return for
+ * atrip's input tensors (src/atrip/Atrip.hpp:68-107): FP64, or interleaved
+ * (re, im) FP64 pairs when the complex flag is 1, in which case every mode
+ * runs the reference's Complex instantiation (src/atrip/Atrip.cxx:1136).
  *
  * Modes
  *   run  [maxit] [ijkabc] [usej] [group]
@@ -17,13 +19,15 @@
  *                                    directly with slices cut as in
  *                                    src/atrip/Unions.hpp:77-278
  *   dump t                        -> Tijk and Zijk of tuple t
- * Output lines start with RESULT / TUPLE / TIJK / ZIJK for easy parsing.
+ * Output lines start with RESULT / TUPLE / TIJK / ZIJK for easy parsing
+ * (complex Tijk/Zijk values print as "re im").
  */
 #include <atrip.hpp>
 #include <atrip/Equations.hpp>
 #include <atrip/Tuples.hpp>
 
 #include <chrono>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -32,49 +36,60 @@
 
 using atrip::Atrip;
 
-static std::vector<double> load(const std::string &dir, const char *name, size_t n) {
-  std::vector<double> v(n);
+template <typename F>
+static std::vector<F> load(const std::string &dir, const char *name, size_t n) {
+  std::vector<F> v(n);
   std::string path = dir + "/" + name + ".bin";
   FILE *f = std::fopen(path.c_str(), "rb");
   if (!f) { std::fprintf(stderr, "cannot open %s\n", path.c_str()); std::exit(2); }
-  if (std::fread(v.data(), sizeof(double), n, f) != n) {
+  if (std::fread(v.data(), sizeof(F), n, f) != n) {
     std::fprintf(stderr, "short read %s\n", path.c_str()); std::exit(2);
   }
   std::fclose(f);
   return v;
 }
 
+template <typename F>
 struct Inputs {
   int No = 0, Nv = 0, hasJ = 0;
-  std::vector<double> epsi, epsa, Tai, Tabij, Vabij, Vijka, Vabci, Jijka, Jabci;
+  std::vector<F> epsi, epsa, Tai, Tabij, Vabij, Vijka, Vabci, Jijka, Jabci;
 };
 
-static Inputs read_inputs(const std::string &dir) {
-  Inputs in;
-  std::ifstream meta(dir + "/meta.txt");
-  meta >> in.No >> in.Nv >> in.hasJ;
-  const size_t No = in.No, Nv = in.Nv;
-  in.epsi = load(dir, "epsi", No);
-  in.epsa = load(dir, "epsa", Nv);
-  in.Tai = load(dir, "Tai", Nv * No);
-  in.Tabij = load(dir, "Tabij", Nv * Nv * No * No);
-  in.Vabij = load(dir, "Vabij", Nv * Nv * No * No);
-  in.Vijka = load(dir, "Vijka", No * No * No * Nv);
-  in.Vabci = load(dir, "Vabci", Nv * Nv * Nv * No);
+template <typename F>
+static Inputs<F> read_inputs(const std::string &dir, int No, int Nv, int hasJ) {
+  Inputs<F> in;
+  in.No = No;
+  in.Nv = Nv;
+  in.hasJ = hasJ;
+  const size_t o = No, v = Nv;
+  in.epsi = load<F>(dir, "epsi", o);
+  in.epsa = load<F>(dir, "epsa", v);
+  in.Tai = load<F>(dir, "Tai", v * o);
+  in.Tabij = load<F>(dir, "Tabij", v * v * o * o);
+  in.Vabij = load<F>(dir, "Vabij", v * v * o * o);
+  in.Vijka = load<F>(dir, "Vijka", o * o * o * v);
+  in.Vabci = load<F>(dir, "Vabci", v * v * v * o);
   if (in.hasJ) {
-    in.Jijka = load(dir, "Jijka", No * No * No * Nv);
-    in.Jabci = load(dir, "Jabci", Nv * Nv * Nv * No);
+    in.Jijka = load<F>(dir, "Jijka", o * o * o * v);
+    in.Jabci = load<F>(dir, "Jabci", v * v * v * o);
   }
   return in;
 }
 
-static CTF::Tensor<double> *make(std::vector<int> lens, const std::vector<double> &v) {
-  auto *t = new CTF::Tensor<double>((int)lens.size(), lens.data());
+template <typename F>
+static CTF::Tensor<F> *make(std::vector<int> lens, const std::vector<F> &v) {
+  auto *t = new CTF::Tensor<F>((int)lens.size(), lens.data());
   std::copy(v.begin(), v.end(), t->data);
   return t;
 }
 
-static int mode_run(const Inputs &in, size_t maxit, bool ijkabc, bool usej, bool group) {
+static void print_value(const char *tag, double x) { std::printf("%s %.17g\n", tag, x); }
+static void print_value(const char *tag, const std::complex<double> &x) {
+  std::printf("%s %.17g %.17g\n", tag, x.real(), x.imag());
+}
+
+template <typename F>
+static int mode_run(const Inputs<F> &in, size_t maxit, bool ijkabc, bool usej, bool group) {
   const int No = in.No, Nv = in.Nv;
   Atrip::init(MPI_COMM_WORLD);
   auto *ei = make({No}, in.epsi), *ea = make({Nv}, in.epsa),
@@ -82,8 +97,8 @@ static int mode_run(const Inputs &in, size_t maxit, bool ijkabc, bool usej, bool
        *Vpphh = make({Nv, Nv, No, No}, in.Vabij),
        *Vhhhp = make({No, No, No, Nv}, in.Vijka),
        *Vppph = make({Nv, Nv, Nv, No}, in.Vabci);
-  CTF::Tensor<double> *Jhhhp = nullptr, *Jppph = nullptr;
-  auto input = Atrip::Input<double>()
+  CTF::Tensor<F> *Jhhhp = nullptr, *Jppph = nullptr;
+  auto input = Atrip::Input<F>()
                    .with_epsilon_i(ei)
                    .with_epsilon_a(ea)
                    .with_Tai(Tph)
@@ -97,25 +112,27 @@ static int mode_run(const Inputs &in, size_t maxit, bool ijkabc, bool usej, bool
                    .with_checkpoint_at_every_iteration(~size_t(0) >> 1)
                    .with_checkpoint_path("/dev/null");
   if (group)
-    input.with_tuples_distribution(Atrip::Input<double>::TuplesDistribution::GROUP_AND_SORT);
+    input.with_tuples_distribution(Atrip::Input<F>::TuplesDistribution::GROUP_AND_SORT);
   if (usej && in.hasJ) {
     Jhhhp = make({No, No, No, Nv}, in.Jijka);
     Jppph = make({Nv, Nv, Nv, No}, in.Jabci);
     input.with_Jijka(Jhhhp).with_Jabci(Jppph);
   }
   auto t0 = std::chrono::steady_clock::now();
-  Atrip::Output out = Atrip::run<double>(input);
+  Atrip::Output out = Atrip::run<F>(input);
   double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   std::printf("RESULT %.17g %.17g %.6f\n", out.energy, out.ct_energy, secs);
   return 0;
 }
 
+template <typename F>
 struct SliceSet {
-  std::vector<double> V[6], Vh[3], Ta[3], Tab[3];
+  std::vector<F> V[6], Vh[3], Ta[3], Tab[3];
 };
 
-static void cut(const Inputs &in, const std::vector<double> &Vp, const std::vector<double> &Vh,
-                size_t a, size_t b, size_t c, SliceSet &s) {
+template <typename F>
+static void cut(const Inputs<F> &in, const std::vector<F> &Vp, const std::vector<F> &Vh,
+                size_t a, size_t b, size_t c, SliceSet<F> &s) {
   const size_t No = in.No, Nv = in.Nv;
   const size_t pairs[6][2] = {{a, b}, {a, c}, {b, c}, {b, a}, {c, a}, {c, b}};
   for (int p = 0; p < 6; ++p) {
@@ -143,8 +160,9 @@ static void cut(const Inputs &in, const std::vector<double> &Vp, const std::vect
   }
 }
 
-static void doubles(const Inputs &in, SliceSet &s, double *Tijk, double *tb, double *vh) {
-  atrip::doubles_contribution<double>(in.No, in.Nv,
+template <typename F>
+static void doubles(const Inputs<F> &in, SliceSet<F> &s, F *Tijk, F *tb, F *vh) {
+  atrip::doubles_contribution<F>(in.No, in.Nv,
       s.V[0].data(), s.V[1].data(), s.V[2].data(), s.V[3].data(), s.V[4].data(), s.V[5].data(),
       s.Vh[0].data(), s.Vh[1].data(), s.Vh[2].data(),
       s.Ta[0].data(), s.Ta[1].data(), s.Ta[2].data(),
@@ -153,18 +171,19 @@ static void doubles(const Inputs &in, SliceSet &s, double *Tijk, double *tb, dou
 
 /* One tuple through the reference's own kernels, in the order of
  * src/atrip/Atrip.cxx:855-963. */
-static void tuple_energy(const Inputs &in, size_t a, size_t b, size_t c, bool ijkabc, bool usej,
-                         double &e, double &ect, std::vector<double> *dumpT = nullptr,
-                         std::vector<double> *dumpZ = nullptr) {
+template <typename F>
+static void tuple_energy(const Inputs<F> &in, size_t a, size_t b, size_t c, bool ijkabc,
+                         bool usej, double &e, double &ect, std::vector<F> *dumpT = nullptr,
+                         std::vector<F> *dumpZ = nullptr) {
   const size_t No = in.No, Nv = in.Nv, n3 = No * No * No;
-  std::vector<double> Tijk(n3), Zijk(n3), tb(n3), vh(n3), Tai(in.Tai);
+  std::vector<F> Tijk(n3), Zijk(n3), tb(n3), vh(n3), Tai(in.Tai);
   if (ijkabc) for (auto &x : Tai) x = -x;
-  std::vector<double> epsi(in.epsi);
-  SliceSet s;
+  std::vector<F> epsi(in.epsi);
+  SliceSet<F> s;
   cut(in, in.Vabci, in.Vijka, a, b, c, s);
   doubles(in, s, Tijk.data(), tb.data(), vh.data());
   Zijk = Tijk;
-  std::vector<double> VAB(No * No), VAC(No * No), VBC(No * No);
+  std::vector<F> VAB(No * No), VAC(No * No), VBC(No * No);
   for (size_t j = 0; j < No; ++j)
     for (size_t i = 0; i < No; ++i) {
       const size_t o = i * Nv * Nv + j * Nv * Nv * No;
@@ -172,29 +191,64 @@ static void tuple_energy(const Inputs &in, size_t a, size_t b, size_t c, bool ij
       VAC[i + j * No] = in.Vabij[a + c * Nv + o];
       VBC[i + j * No] = in.Vabij[b + c * Nv + o];
     }
-  atrip::singles_contribution<double>(No, Nv, a, b, c, Tai.data(), VAB.data(), VAC.data(),
-                                      VBC.data(), Zijk.data());
+  atrip::singles_contribution<F>(No, Nv, a, b, c, Tai.data(), VAB.data(), VAC.data(),
+                                 VBC.data(), Zijk.data());
   if (dumpT) *dumpT = Tijk;
   if (dumpZ) *dumpZ = Zijk;
-  const double epsabc = in.epsa[a] + in.epsa[b] + in.epsa[c];
+  // src/atrip/Atrip.cxx:640-646: real part of the sum, as a field value
+  const F epsabc{std::real(in.epsa[a] + in.epsa[b] + in.epsa[c])};
   int distinct = 0;
   if (a == b) distinct++;
   if (b == c) distinct--;
-  auto energy = [&](double *T) {
+  auto energy = [&](F *T) {
     double r = 0.0;
     if (distinct == 0)
-      atrip::get_energy_distinct<double>(epsabc, No, epsi.data(), T, Zijk.data(), &r);
+      atrip::get_energy_distinct<F>(epsabc, No, epsi.data(), T, Zijk.data(), &r);
     else
-      atrip::get_energy_same<double>(epsabc, No, epsi.data(), T, Zijk.data(), &r);
+      atrip::get_energy_same<F>(epsabc, No, epsi.data(), T, Zijk.data(), &r);
     return r;
   };
   e = energy(Tijk.data());
   if (usej && in.hasJ) {
-    SliceSet sj;
+    SliceSet<F> sj;
     cut(in, in.Jabci, in.Jijka, a, b, c, sj);
     doubles(in, sj, Tijk.data(), tb.data(), vh.data());
   }
   ect = energy(Tijk.data());
+}
+
+template <typename F>
+static int main_t(const std::string &dir, const std::string &mode, int No, int Nv, int hasJ,
+                  int argc, char **argv) {
+  Inputs<F> in = read_inputs<F>(dir, No, Nv, hasJ);
+  auto arg = [&](int i, long dflt) { return argc > i ? std::atol(argv[i]) : dflt; };
+  if (mode == "run")
+    return mode_run(in, (size_t)arg(3, 0), arg(4, 0) != 0, arg(5, 1) != 0, arg(6, 0) != 0);
+  if (mode == "tuples") {
+    const size_t n = (size_t)arg(3, 10);
+    const bool ijkabc = arg(4, 0) != 0, usej = arg(5, 1) != 0;
+    auto all = atrip::get_all_tuples_list(in.Nv);
+    for (size_t t = 0; t < n && t < all.size(); ++t) {
+      double e, ect;
+      tuple_energy(in, all[t][0], all[t][1], all[t][2], ijkabc, usej, e, ect);
+      std::printf("TUPLE %zu %zu %zu %zu %.17g %.17g\n", t, all[t][0], all[t][1], all[t][2], e,
+                  ect);
+    }
+    return 0;
+  }
+  if (mode == "dump") {
+    const size_t t = (size_t)arg(3, 0);
+    auto all = atrip::get_all_tuples_list(in.Nv);
+    std::vector<F> T, Z;
+    double e, ect;
+    tuple_energy(in, all[t][0], all[t][1], all[t][2], false, false, e, ect, &T, &Z);
+    for (const F &x : T) print_value("TIJK", x);
+    for (const F &x : Z) print_value("ZIJK", x);
+    std::printf("TUPLE %zu %zu %zu %zu %.17g %.17g\n", t, all[t][0], all[t][1], all[t][2], e, ect);
+    return 0;
+  }
+  std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
+  return 2;
 }
 
 int main(int argc, char **argv) {
@@ -203,33 +257,15 @@ int main(int argc, char **argv) {
     return 2;
   }
   const std::string dir = argv[1], mode = argv[2];
-  Inputs in = read_inputs(dir);
-  auto arg = [&](int i, long dflt) { return argc > i ? std::atol(argv[i]) : dflt; };
+  int No = 0, Nv = 0, hasJ = 0, cplx = 0;
+  {
+    std::ifstream meta(dir + "/meta.txt");
+    meta >> No >> Nv >> hasJ;
+    if (!(meta >> cplx)) cplx = 0;
+  }
   try {
-    if (mode == "run")
-      return mode_run(in, (size_t)arg(3, 0), arg(4, 0) != 0, arg(5, 1) != 0, arg(6, 0) != 0);
-    if (mode == "tuples") {
-      const size_t n = (size_t)arg(3, 10);
-      const bool ijkabc = arg(4, 0) != 0, usej = arg(5, 1) != 0;
-      auto all = atrip::get_all_tuples_list(in.Nv);
-      for (size_t t = 0; t < n && t < all.size(); ++t) {
-        double e, ect;
-        tuple_energy(in, all[t][0], all[t][1], all[t][2], ijkabc, usej, e, ect);
-        std::printf("TUPLE %zu %zu %zu %zu %.17g %.17g\n", t, all[t][0], all[t][1], all[t][2], e, ect);
-      }
-      return 0;
-    }
-    if (mode == "dump") {
-      const size_t t = (size_t)arg(3, 0);
-      auto all = atrip::get_all_tuples_list(in.Nv);
-      std::vector<double> T, Z;
-      double e, ect;
-      tuple_energy(in, all[t][0], all[t][1], all[t][2], false, false, e, ect, &T, &Z);
-      for (double x : T) std::printf("TIJK %.17g\n", x);
-      for (double x : Z) std::printf("ZIJK %.17g\n", x);
-      std::printf("TUPLE %zu %zu %zu %zu %.17g %.17g\n", t, all[t][0], all[t][1], all[t][2], e, ect);
-      return 0;
-    }
+    if (cplx) return main_t<atrip::Complex>(dir, mode, No, Nv, hasJ, argc, argv);
+    return main_t<double>(dir, mode, No, Nv, hasJ, argc, argv);
   } catch (const char *m) {
     std::fprintf(stderr, "reference threw: %s\n", m);
     return 3;
@@ -237,6 +273,4 @@ int main(int argc, char **argv) {
     std::fprintf(stderr, "reference threw: %s\n", m.c_str());
     return 3;
   }
-  std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
-  return 2;
 }

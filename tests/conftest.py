@@ -32,9 +32,11 @@ _INPUT_CACHE = {}
 def golden_inputs(fx):
     """Inputs of a fixture, regenerated from its seed (cached per session)."""
     from atrip_gb300 import synth
-    key = (fx["No"], fx["Nv"], fx["seed"], fx["with_j"])
+    key = (fx["No"], fx["Nv"], fx["seed"], fx["with_j"], fx.get("field", "real"),
+           fx.get("eps_imag", 0.0))
     if key not in _INPUT_CACHE:
         if len(_INPUT_CACHE) > 4:
             _INPUT_CACHE.clear()
-        _INPUT_CACHE[key] = synth.make_inputs(*key[:3], with_j=key[3])
+        _INPUT_CACHE[key] = synth.make_inputs(*key[:3], with_j=key[3], field=key[4],
+                                              eps_imag=key[5])
     return _INPUT_CACHE[key]

@@ -47,8 +47,12 @@ def test_oracle_tuple_arrays_match_reference(name):
     t = fx["dump"]["t"]
     a, b, c = oracle.tuple_list(fx["Nv"])[t]
     T, Z = oracle.tuple_arrays(p, a, b, c)
-    np.testing.assert_allclose(T, fx["dump"]["Tijk"], rtol=1e-12, atol=1e-15)
-    np.testing.assert_allclose(Z, fx["dump"]["Zijk"], rtol=1e-12, atol=1e-15)
+
+    def ref(v):
+        v = np.array(v)
+        return v[:, 0] + 1j * v[:, 1] if v.ndim == 2 else v  # complex: [re, im] pairs
+    np.testing.assert_allclose(T, ref(fx["dump"]["Tijk"]), rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(Z, ref(fx["dump"]["Zijk"]), rtol=1e-12, atol=1e-15)
 
 
 def test_tuple_count_and_order():
@@ -68,3 +72,15 @@ def test_naive_and_port_routes_agree_with_j():
     a = oracle.run(p, route="naive", threads=2)
     b = oracle.run(p, route="port", threads=3)
     assert _close(a[0], b[0], a[0]) and _close(a[1], b[1], a[0])
+
+
+def test_complex_field_is_not_the_real_one():
+    """The complex fixtures exercise the conjugations: dropping the imaginary
+    parts changes the energies, and the reference's two routes (DGEMM with
+    the hole conjugation, naive loops without) disagree for complex input."""
+    fx = load_golden("z_odd_no5_nv7_s2_j_epsim")
+    d = golden_inputs(fx)
+    real = {k: (np.real(v) if isinstance(v, np.ndarray) else v) for k, v in d.items()}
+    e_real, _ = oracle.run(oracle.Problem(real), use_j=True)
+    assert abs(e_real - fx["energy"]) > 1e-6 * abs(fx["energy"])
+    assert abs(fx["energy_naive_variant"] - fx["energy"]) > 1e-9 * abs(fx["energy"])
