@@ -199,14 +199,28 @@ def _lens(t):
     return list(t.shape)
 
 
-def _payload(t):
+def _payload(t, complex_field: bool = False):
     """numpy/torch arrays pass through; CTF-like objects are read_all'ed."""
     if hasattr(t, "read_all") and not hasattr(t, "shape"):
         n = int(np.prod(_lens(t)))
-        buf = np.empty(n, dtype=np.float64)
+        buf = np.empty(n, dtype=np.complex128 if complex_field else np.float64)
         t.read_all(buf)
         return buf
     return t
+
+
+def _is_complex(t) -> bool:
+    """Field of an input: complex dtype (numpy/torch) or a CTF-like object
+    that says so through ``is_complex`` / ``dtype``."""
+    if getattr(t, "is_complex", None) is True:
+        return True
+    dt = getattr(t, "dtype", None)
+    if dt is None:
+        return False
+    try:
+        return bool(np.issubdtype(np.dtype(dt), np.complexfloating))
+    except TypeError:
+        return "complex" in str(dt)
 
 
 class Atrip:
@@ -231,12 +245,15 @@ class Atrip:
             raise ValueError("epsilon_i and epsilon_a are required")
         No, Nv = _lens(inp.ei)[0], _lens(inp.ea)[0]
         t_start = time.perf_counter()
-        with capi.Context(No, Nv, inp.device) as ctx:
+        # run<Complex> (src/atrip/Atrip.cxx:1136) when the inputs are complex
+        cplx = any(_is_complex(getattr(inp, attr)) for attr, _ in _TENSORS.values()
+                   if getattr(inp, attr) is not None)
+        with capi.Context(No, Nv, inp.device, field="complex" if cplx else "real") as ctx:
             for key, (attr, cname) in _TENSORS.items():
                 t = getattr(inp, attr)
                 if t is None:
                     continue
-                ctx.upload(cname, _payload(t))
+                ctx.upload(cname, _payload(t, cplx))
             if inp.delete_Vppph:
                 inp.Vppph = None  # the caller's V_pphp is dropped as in src/atrip/Atrip.cxx:310
             n = capi.n_tuples(Nv)

@@ -37,9 +37,13 @@ class AtripError(RuntimeError):
         self.status = status
 
 
+# enum atrip_field
+FIELD_REAL, FIELD_COMPLEX = range(2)
+
+
 class Dims(ctypes.Structure):
     _fields_ = [("no", ctypes.c_int32), ("nv", ctypes.c_int32), ("device", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("field", ctypes.c_int32)]
 
 
 class RunOptions(ctypes.Structure):
@@ -149,17 +153,19 @@ def measure_peaks(device: int = 0):
 class Context:
     """One GPU's engine state (wraps atrip_gpu_context)."""
 
-    def __init__(self, No: int, Nv: int, device: int = 0):
+    def __init__(self, No: int, Nv: int, device: int = 0, field: str = "real"):
         self.lib = load()
-        self.No, self.Nv, self.device = No, Nv, device
+        self.No, self.Nv, self.device, self.field = No, Nv, device, field
+        f = {"real": FIELD_REAL, "complex": FIELD_COMPLEX}[field]
         h = ctypes.c_void_p()
-        check(self.lib.atrip_gpu_create(ctypes.byref(Dims(No, Nv, device, 0)), ctypes.byref(h)))
+        check(self.lib.atrip_gpu_create(ctypes.byref(Dims(No, Nv, device, f)), ctypes.byref(h)))
         self.h = h
 
     def upload(self, name: str, array) -> None:
         """Upload a tensor: a numpy array (column-major data, any memory
         order of the logical array) or a CUDA torch tensor holding the
-        column-major data as one contiguous buffer."""
+        column-major data as one contiguous buffer (complex128 for a complex
+        context)."""
         tid = TENSOR_IDS[name]
         mod = type(array).__module__
         if mod.startswith("torch") and array.is_cuda:
@@ -168,7 +174,8 @@ class Context:
                                                    t.numel()))
             return
         import numpy as np
-        a = np.asarray(array, dtype=np.float64)
+        dtype = np.complex128 if self.field == "complex" else np.float64
+        a = np.asarray(array, dtype=dtype)
         flat = np.ascontiguousarray(a.ravel(order="F"))
         check(self.lib.atrip_gpu_upload(self.h, tid, flat.ctypes.data, flat.size))
 

@@ -142,6 +142,8 @@ int atrip_gpu_batch_create(atrip_gpu_context *const *systems, int32_t n, atrip_g
     if (!systems[s]) return fail(ATRIP_ERR_ARGUMENT, "null system " + std::to_string(s));
     if (systems[s]->device != systems[0]->device)
       return fail(ATRIP_ERR_ARGUMENT, "systems live on different devices");
+    if (systems[s]->field != ATRIP_FIELD_REAL)
+      return fail(ATRIP_ERR_UNSUPPORTED, "batches hold real-field systems only");
     if (systems[s]->No > kBatchMaxNo)
       return fail(ATRIP_ERR_UNSUPPORTED, "batch systems need No <= " + std::to_string(kBatchMaxNo));
     for (int t = 0; t < s; ++t)

@@ -124,16 +124,18 @@ int upload_impl(atrip_gpu_context *c, int32_t tensor, const double *src, int64_t
   ATRIP_CUDA_TRY(cudaSetDevice(c->device));
   if (c->have[tensor]) free_tensor(c, tensor);
   const cudaMemcpyKind kind = src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const bool cplx = c->field == ATRIP_FIELD_COMPLEX;
+  const size_t elem = sizeof(double) * (cplx ? 2 : 1);
   if (double **d = direct_slot(c, tensor)) {
-    ATRIP_CUDA_TRY(cudaMalloc(d, sizeof(double) * std::max<int64_t>(n, 1)));
-    ATRIP_CUDA_TRY(cudaMemcpyAsync(*d, src, sizeof(double) * n, kind, c->stream));
+    ATRIP_CUDA_TRY(cudaMalloc(d, elem * std::max<int64_t>(n, 1)));
+    ATRIP_CUDA_TRY(cudaMemcpyAsync(*d, src, elem * n, kind, c->stream));
   } else {
     PermutePlan p = plan_for(c, tensor);
     const double *colmajor = src;
     double *staging = nullptr;
     if (!src_on_device) {
-      ATRIP_CUDA_TRY(cudaMalloc(&staging, sizeof(double) * std::max<int64_t>(n, 1)));
-      cudaError_t e = cudaMemcpyAsync(staging, src, sizeof(double) * n, kind, c->stream);
+      ATRIP_CUDA_TRY(cudaMalloc(&staging, elem * std::max<int64_t>(n, 1)));
+      cudaError_t e = cudaMemcpyAsync(staging, src, elem * n, kind, c->stream);
       if (e != cudaSuccess) {
         cudaFree(staging);
         ATRIP_CUDA_TRY(e);
@@ -141,8 +143,9 @@ int upload_impl(atrip_gpu_context *c, int32_t tensor, const double *src, int64_t
       colmajor = staging;
     }
     for (int i = 0; i < p.count; ++i) {
-      cudaError_t e = cudaMalloc(p.dst[i], sizeof(double) * std::max<int64_t>(n, 1));
-      if (e == cudaSuccess) e = launch_permute4(*p.dst[i], colmajor, p.n[i], p.s[i], c->stream);
+      cudaError_t e = cudaMalloc(p.dst[i], elem * std::max<int64_t>(n, 1));
+      if (e == cudaSuccess)
+        e = launch_permute4(*p.dst[i], colmajor, p.n[i], p.s[i], c->stream, cplx);
       if (e != cudaSuccess) {
         if (staging) {
           cudaStreamSynchronize(c->stream);
@@ -211,6 +214,8 @@ int atrip_gpu_create(const atrip_dims *dims, atrip_gpu_context **out) {
     return fail(ATRIP_ERR_UNSUPPORTED, "No must be in [1, 64], got " + std::to_string(dims->no));
   if (dims->nv < 1 || dims->nv > 1023)
     return fail(ATRIP_ERR_UNSUPPORTED, "Nv must be in [1, 1023], got " + std::to_string(dims->nv));
+  if (dims->field != ATRIP_FIELD_REAL && dims->field != ATRIP_FIELD_COMPLEX)
+    return fail(ATRIP_ERR_ARGUMENT, "unknown field " + std::to_string(dims->field));
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(ATRIP_ERR_NO_DEVICE, "no CUDA device visible");
@@ -227,6 +232,7 @@ int atrip_gpu_create(const atrip_dims *dims, atrip_gpu_context **out) {
   c->No = dims->no;
   c->Nv = dims->nv;
   c->device = dims->device;
+  c->field = dims->field;
   c->sm_count = prop.multiProcessorCount;
   c->n_tuples = atrip_gpu_n_tuples(c->Nv);
   auto bail = [&](int code) {
@@ -316,7 +322,11 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
   if (opts->max_iterations != 0) t_end = std::min<int64_t>(t_end, opts->max_iterations + 1);
   const int64_t t_begin = std::min<int64_t>(opts->first_iteration, t_end);
   const int64_t n = t_end - t_begin;
-  int form = opts->form == ATRIP_FORM_AUTO ? ATRIP_FORM_SPLIT_BF16 : opts->form;
+  const bool cplx = c->field == ATRIP_FIELD_COMPLEX;
+  int form = opts->form == ATRIP_FORM_AUTO ? (cplx ? ATRIP_FORM_FP64 : ATRIP_FORM_SPLIT_BF16)
+                                           : opts->form;
+  if (cplx && form != ATRIP_FORM_FP64)
+    return fail(ATRIP_ERR_UNSUPPORTED, "complex field: only the FP64 form is built");
   int slices = opts->slices > 0 ? opts->slices : 3;
   int64_t launches = 0;
   ATRIP_CUDA_TRY(cudaEventRecord(c->ev0, st));
@@ -325,10 +335,11 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
     if (form == ATRIP_FORM_FP64) {
       const int rows_tile = c->tune.fp64_tile_rows == 32 ? 32 : 64;
       const int min_blocks = c->tune.fp64_min_blocks == 2 ? 2 : 0;
-      int per_sm = std::max(1, triples_fp64_max_blocks_per_sm(c->No, rows_tile, min_blocks));
+      int per_sm = std::max(1, cplx ? triples_z_max_blocks_per_sm(c->No)
+                                    : triples_fp64_max_blocks_per_sm(c->No, rows_tile, min_blocks));
       if (c->tune.fp64_ctas_per_sm > 0) per_sm = std::min(per_sm, (int)c->tune.fp64_ctas_per_sm);
       const int64_t grid = std::min<int64_t>((int64_t)c->sm_count * per_sm, n);
-      const size_t ws = (size_t)grid * 2 * (size_t)c->No * c->No * c->No;
+      const size_t ws = (size_t)grid * 2 * (cplx ? 2 : 1) * (size_t)c->No * c->No * c->No;
       if (ws > c->workspace_doubles) {
         cudaFree(c->d_workspace);
         c->d_workspace = nullptr;
@@ -363,7 +374,10 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
       a.rows_tile = rows_tile;
       a.claim = std::max(1, (int)c->tune.tuples_per_claim);
       a.min_blocks = min_blocks;
-      ATRIP_CUDA_TRY(launch_triples_fp64(a, (int)grid, st));
+      if (cplx)
+        ATRIP_CUDA_TRY(launch_triples_z(a, (int)grid, st));
+      else
+        ATRIP_CUDA_TRY(launch_triples_fp64(a, (int)grid, st));
       launches += 1;
     } else {
       c->split.stage_cap = c->tune.split_stages;

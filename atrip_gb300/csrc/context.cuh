@@ -12,6 +12,7 @@
 
 struct atrip_gpu_context {
   int No = 0, Nv = 0, device = 0, sm_count = 0;
+  int field = ATRIP_FIELD_REAL;  // enum atrip_field: doubles per element = 1 + field
   int64_t n_tuples = 0;
   int n_triples = 0;
   bool have[ATRIP_N_TENSORS] = {};

@@ -76,9 +76,15 @@ cudaError_t launch_batch_energy_sum(const BatchArgs &b, double *sums, cudaStream
 int triples_fp64_max_blocks_per_sm(int No, int rows_tile, int min_blocks);
 int triples_fp64_batch_max_blocks_per_sm(int max_no, int min_blocks);
 
-// dst[i0 + n0 (i1 + n1 (i2 + n2 i3))] = src[i0 s0 + i1 s1 + i2 s2 + i3 s3]
+// dst[i0 + n0 (i1 + n1 (i2 + n2 i3))] = src[i0 s0 + i1 s1 + i2 s2 + i3 s3],
+// elements of one double, or of two (re, im) when complex_elems
 cudaError_t launch_permute4(double *dst, const double *src, const int64_t n[4],
-                            const int64_t s[4], cudaStream_t st);
+                            const int64_t s[4], cudaStream_t st, bool complex_elems);
+
+// Complex field: the same launch arguments, every tensor pointer holding
+// interleaved (re, im) pairs, workspace 4 No^3 doubles per CTA.
+cudaError_t launch_triples_z(const TriplesArgs &a, int grid, cudaStream_t s);
+int triples_z_max_blocks_per_sm(int No);
 
 // Compensated two-stage sum of x[0..n) and y[0..n) into out[0], out[1].
 cudaError_t launch_energy_sum(const double *x, const double *y, int64_t n, double *partials,

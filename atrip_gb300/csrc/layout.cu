@@ -14,7 +14,8 @@ namespace {
 
 // 4-D permutation as a gather: coalesced stores, strided loads.  Runs once
 // per uploaded tensor.
-__global__ void permute4_kernel(double *__restrict__ dst, const double *__restrict__ src,
+template <typename T>
+__global__ void permute4_kernel(T *__restrict__ dst, const T *__restrict__ src,
                                 int64_t n0, int64_t n1, int64_t n2, int64_t n3, int64_t s0,
                                 int64_t s1, int64_t s2, int64_t s3) {
   const int64_t total = n0 * n1 * n2 * n3;
@@ -93,13 +94,18 @@ __global__ void energy_sum_stage2(const double *__restrict__ partials, int nb,
 }  // namespace
 
 cudaError_t launch_permute4(double *dst, const double *src, const int64_t n[4], const int64_t s[4],
-                            cudaStream_t st) {
+                            cudaStream_t st, bool complex_elems) {
   const int64_t total = n[0] * n[1] * n[2] * n[3];
   if (total == 0) return cudaSuccess;
   int64_t blocks = (total + 255) / 256;
   if (blocks > 152 * 64) blocks = 152 * 64;
-  permute4_kernel<<<(int)blocks, 256, 0, st>>>(dst, src, n[0], n[1], n[2], n[3], s[0], s[1], s[2],
-                                               s[3]);
+  if (complex_elems)
+    permute4_kernel<double2><<<(int)blocks, 256, 0, st>>>(
+        reinterpret_cast<double2 *>(dst), reinterpret_cast<const double2 *>(src), n[0], n[1],
+        n[2], n[3], s[0], s[1], s[2], s[3]);
+  else
+    permute4_kernel<double><<<(int)blocks, 256, 0, st>>>(dst, src, n[0], n[1], n[2], n[3], s[0],
+                                                         s[1], s[2], s[3]);
   return cudaGetLastError();
 }
 

@@ -182,6 +182,10 @@ struct Atrip {
 
   template <typename F = double>
   static Output run(Input<F> const &in);
+
+ private:
+  template <typename F>
+  static Output run_field(Input<F> const &in, int32_t field);
 };
 
 namespace detail {
@@ -191,8 +195,8 @@ inline void check(int status) {
 }
 
 template <typename F>
-inline std::vector<double> gather(CTF::Tensor<F> *t, size_t expected) {
-  std::vector<double> buf(expected);
+inline std::vector<F> gather(CTF::Tensor<F> *t, size_t expected) {
+  std::vector<F> buf(expected);
   t->read_all(buf.data());
   return buf;
 }
@@ -204,19 +208,21 @@ struct ContextGuard {
 
 }  // namespace detail
 
-// src/atrip/Atrip.cxx:66-1133 on one GPU.
-template <>
-inline Atrip::Output Atrip::run<double>(Atrip::Input<double> const &in) {
+// src/atrip/Atrip.cxx:66-1133 on one GPU, for F = double or Complex
+// (std::complex<double> is laid out as (re, im), what the C ABI takes for
+// ATRIP_FIELD_COMPLEX).
+template <typename F>
+inline Atrip::Output Atrip::run_field(Atrip::Input<F> const &in, int32_t field) {
   using clock = std::chrono::steady_clock;
   const auto t_start = clock::now();
   if (!in.ei || !in.ea || !in.Tph || !in.Tpphh || !in.Vpphh || !in.Vhhhp || !in.Vppph)
     throw std::string("atrip_gb300: Atrip::run needs ei, ea, Tai, Tabij, Vabij, Vijka, Vabci");
   const size_t No = in.ei->lens[0], Nv = in.ea->lens[0];
-  atrip_dims dims{(int32_t)No, (int32_t)Nv, in.device, 0};
+  atrip_dims dims{(int32_t)No, (int32_t)Nv, in.device, field};
   detail::ContextGuard g;
   detail::check(atrip_gpu_create(&dims, &g.c));
   struct Slot {
-    CTF::Tensor<double> *t;
+    CTF::Tensor<F> *t;
     int id;
     size_t n;
   } slots[] = {
@@ -232,8 +238,9 @@ inline Atrip::Output Atrip::run<double>(Atrip::Input<double> const &in) {
   };
   for (auto &s : slots) {
     if (!s.t) continue;
-    std::vector<double> buf = detail::gather(s.t, s.n);
-    detail::check(atrip_gpu_upload(g.c, s.id, buf.data(), (int64_t)s.n));
+    std::vector<F> buf = detail::gather(s.t, s.n);
+    detail::check(
+        atrip_gpu_upload(g.c, s.id, reinterpret_cast<const double *>(buf.data()), (int64_t)s.n));
   }
   if (in.delete_Vppph) delete in.Vppph;  // src/atrip/Atrip.cxx:310
 
@@ -293,8 +300,14 @@ inline Atrip::Output Atrip::run<double>(Atrip::Input<double> const &in) {
 }
 
 template <>
-inline Atrip::Output Atrip::run<Complex>(Atrip::Input<Complex> const &) {
-  throw std::string("atrip_gb300: the complex field is not built yet");
+inline Atrip::Output Atrip::run<double>(Atrip::Input<double> const &in) {
+  return run_field(in, ATRIP_FIELD_REAL);
+}
+
+// src/atrip/Atrip.cxx:1136: the Complex instantiation (FP64 form).
+template <>
+inline Atrip::Output Atrip::run<Complex>(Atrip::Input<Complex> const &in) {
+  return run_field(in, ATRIP_FIELD_COMPLEX);
 }
 
 }  // namespace atrip

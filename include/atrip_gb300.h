@@ -71,13 +71,20 @@ enum atrip_form {
   ATRIP_FORM_AUTO = 2        /* the context's tuned choice                    */
 };
 
+/* Field of the inputs (atrip's Atrip::run<double> / run<Complex>,
+ * src/atrip/Atrip.cxx:1135-1136). */
+enum atrip_field {
+  ATRIP_FIELD_REAL = 0,    /* FP64 elements                                  */
+  ATRIP_FIELD_COMPLEX = 1  /* std::complex<double>: interleaved (re, im) FP64 */
+};
+
 typedef struct atrip_gpu_context atrip_gpu_context;
 
 typedef struct {
   int32_t no;     /* occupied orbitals, 1 <= no <= 64   */
   int32_t nv;     /* virtual orbitals,  1 <= nv <= 1023 */
   int32_t device; /* CUDA device ordinal                */
-  int32_t reserved;
+  int32_t field;  /* enum atrip_field (0 = real)        */
 } atrip_dims;
 
 /* Options of one run; mirrors the Input attributes that change results or
@@ -112,8 +119,9 @@ typedef struct {
 int atrip_gpu_create(const atrip_dims *dims, atrip_gpu_context **out);
 
 /* Upload one input tensor from host memory (pageable or pinned), n_elements
- * FP64 values in column-major order.  The device copy is kept in the
- * engine's own layout.  Replaces read_all + the SliceUnion constructors
+ * values in column-major order (FP64, or (re, im) FP64 pairs for a complex
+ * context: n_elements counts complex values).  The device copy is kept in
+ * the engine's own layout.  Replaces read_all + the SliceUnion constructors
  * (src/atrip/Atrip.cxx:176-215, 277-362; src/atrip/Unions.hpp:77-278).     */
 int atrip_gpu_upload(atrip_gpu_context *ctx, int32_t tensor, const double *host_colmajor,
                      int64_t n_elements);
