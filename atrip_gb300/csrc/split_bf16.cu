@@ -363,7 +363,11 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t dbase = tmem + buf * K::kBufCols;
           for (int pt = 0; pt < 4 && alive; ++pt) {
             const int nch = (pt & 1) == 0 ? kch : 1;
-            for (int ch = 0; ch < nch && alive; ++ch)
+            for (int ch = 0; ch < nch && alive; ++ch) {
+              // K steps of 16 that hold data: the zero padding past Nv (last
+              // particle chunk) and past No (hole chunk) is skipped
+              const int kvalid = (pt & 1) == 0 ? min(kKChunk, g.Nv - ch * kKChunk) : g.No;
+              const int nkk = (kvalid + 15) / 16;
               for (int sa = 0; sa < S; ++sa) {
                 const int st = unit_count % kStages;
                 const uint32_t use_s = unit_count / kStages;
@@ -381,21 +385,21 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (SPLIT0 && pt >= 2 && sa == 0) {
                   // level 0 of the transposed half has its own accumulator
 #pragma unroll
-                  for (int kk = 0; kk < kKChunk / 16; ++kk)
+                  for (int kk = 0; kk < nkk; ++kk)
                     mma_bf16(dbase + S * NP, adesc + 2 * kk, bdesc + 2 * kk,
                              idesc_bf16_f32(128, NP), (fresh_tr0 && kk == 0) ? 0u : 1u);
                   fresh_tr0 = false;
                   if (S > 1) {
                     const uint64_t bdesc1 = sdesc_sw128(sbase + kATileBytes + K::kBTile);
 #pragma unroll
-                    for (int kk = 0; kk < kKChunk / 16; ++kk)
+                    for (int kk = 0; kk < nkk; ++kk)
                       mma_bf16(dbase + NP, adesc + 2 * kk, bdesc1 + 2 * kk,
                                idesc_bf16_f32(128, (S - 1) * NP), 1u);
                   }
                 } else {
                   const uint32_t id = idesc_bf16_f32(128, (S - sa) * NP);
 #pragma unroll
-                  for (int kk = 0; kk < kKChunk / 16; ++kk)
+                  for (int kk = 0; kk < nkk; ++kk)
                     mma_bf16(dbase + sa * NP, adesc + 2 * kk, bdesc + 2 * kk, id,
                              (fresh_main && kk == 0) ? 0u : 1u);
                   fresh_main = false;
@@ -403,6 +407,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 mma_commit(&empty[st]);
                 ++unit_count;
               }
+            }
           }
           mma_commit(&accf[buf]);
           ++item_count;

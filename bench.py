@@ -330,8 +330,11 @@ def run_single(args, workload, world, rank, local):
     form = args.form
     batch = args.batch_tuples or max(1, int((STEP_FLOPS if form != "fp64" else STEP_FLOPS_FP64)
                                             / fpt))
-    batch = min(batch, n)
-    origin = (rank * batch) % n  # weak scaling: rank r walks its own stretch
+    # the list is cut into `parts` equal stretches of `batch` tuples (the last
+    # one shorter); step s runs stretch (s + rank) % parts (weak scaling:
+    # rank r starts at its own stretch)
+    parts = max(1, round(n / min(batch, n)))
+    batch = -(-n // parts)
 
     ctx = capi.Context(No, Nv, local)
     _upload_all(ctx, d)
@@ -343,9 +346,12 @@ def run_single(args, workload, world, rank, local):
                              slices=args.slices)
     slices = tune["slices"] if form != "fp64" else 0
 
+    def stretch(s):
+        lo = ((s + rank) % parts) * batch
+        return lo, min(n, lo + batch)
+
     def step(s):
-        lo = (origin + s * batch) % n
-        hi = min(n, lo + batch)
+        lo, hi = stretch(s)
         return ctx.run(form=form, slices=slices, use_j=False, first_iteration=lo,
                        max_iterations=hi - 1, stream=stream.cuda_stream)
 
@@ -396,8 +402,7 @@ def run_single(args, workload, world, rank, local):
             c2.set_tuning(**ctx.get_tuning())
             for name in TENSORS:
                 c2.upload_ptr(name, pinned[name].data_ptr(), pinned[name].numel(), False)
-            lo = (origin + s * batch) % n
-            hi = min(n, lo + batch)
+            lo, hi = stretch(s)
             r = c2.run(form=form, slices=slices, use_j=False, first_iteration=lo,
                        max_iterations=hi - 1)
             e2e_tuples += r.tuples_done
@@ -409,11 +414,14 @@ def run_single(args, workload, world, rank, local):
         return 0
     peaks = load_peaks()
     live_fp64 = capi.measure_peaks(local)[0] if form == "fp64" else None
-    kernel_ms = statistics.median(r.device_ms for r in res)
+    # per launch: the steps' mean tuples and mean device time of the loop
+    launch_tuples = tuples / len(res)
+    kernel_ms = sum(r.device_ms for r in res) / len(res)
     kname = "triples_fp64_kernel" if form == "fp64" else "triples_split_kernel"
     tpt = traffic_per_tuple(kname, workload)
-    roof = _roofline(form, slices, batch * fpt, kernel_ms, peaks, live_fp64,
-                     tpt * batch if tpt is not None else None)
+    roof = _roofline(form, slices, launch_tuples * fpt, kernel_ms, peaks, live_fp64,
+                     tpt * launch_tuples if tpt is not None else None)
+    roof["tuples_per_launch"] = launch_tuples
     cpu = None if args.no_cpu_baseline else cpu_baseline(d, args.cpu_seconds)
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
@@ -423,7 +431,7 @@ def run_single(args, workload, world, rank, local):
         "data": "synthetic (seeded, benchmark value distributions)",
         "config": {"workload": f"CCSD(T) triples No={No} Nv={Nv} seed {SEED}", "name": workload,
                    "form": form, "slices": slices, "tuning": tune["tuning"],
-                   "tuples_per_step": batch, "n_tuples": n,
+                   "tuples_per_step": batch, "stretches": parts, "n_tuples": n,
                    "l2": "no flush: inputs > 129 MB L2",
                    "time_to_ET_s": time_to_et, "input_gen_s": t_gen},
         "compare_fp64": compare,
