@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -109,6 +110,17 @@ void free_tensor(atrip_gpu_context *c, int t) {
   split_invalidate(c->split);
 }
 
+// Host uploads above this many elements are staged in chunks (default 2^28
+// elements, 2 GiB of FP64; ATRIP_GB300_STAGING_ELEMS overrides it).
+int64_t staging_elems() {
+  static const int64_t v = [] {
+    const char *e = std::getenv("ATRIP_GB300_STAGING_ELEMS");
+    const long long x = e ? std::atoll(e) : 0;
+    return x > 0 ? (int64_t)x : (int64_t(1) << 28);
+  }();
+  return v;
+}
+
 int upload_impl(atrip_gpu_context *c, int32_t tensor, const double *src, int64_t n,
                 bool src_on_device) {
   clear_error();
@@ -129,6 +141,52 @@ int upload_impl(atrip_gpu_context *c, int32_t tensor, const double *src, int64_t
   if (double **d = direct_slot(c, tensor)) {
     ATRIP_CUDA_TRY(cudaMalloc(d, elem * std::max<int64_t>(n, 1)));
     ATRIP_CUDA_TRY(cudaMemcpyAsync(*d, src, elem * n, kind, c->stream));
+  } else if (!src_on_device && n > staging_elems()) {
+    // Large host tensor: stream it through a bounded staging buffer, a run
+    // of values of the source's slowest index at a time, so the upload
+    // needs the destination layouts plus at most kStagingElems elements.
+    PermutePlan p = plan_for(c, tensor);
+    const double *hsrc = src;
+    for (int i = 0; i < p.count; ++i)
+      ATRIP_CUDA_TRY(cudaMalloc(p.dst[i], elem * std::max<int64_t>(n, 1)));
+    int dslow[2];
+    int64_t m = 0, S = 0;
+    for (int i = 0; i < p.count; ++i) {
+      int d = 0;
+      for (int k = 1; k < 4; ++k)
+        if (p.s[i][k] > p.s[i][d]) d = k;
+      dslow[i] = d;
+      m = p.n[i][d];
+      S = p.s[i][d];  // every plan of one tensor has the same source
+    }
+    const int64_t cv = std::max<int64_t>(1, staging_elems() / S);
+    double *staging = nullptr;
+    ATRIP_CUDA_TRY(cudaMalloc(&staging, elem * std::min<int64_t>(n, cv * S)));
+    int rc = ATRIP_OK;
+    for (int64_t v0 = 0; v0 < m && rc == ATRIP_OK; v0 += cv) {
+      const int64_t nv = std::min<int64_t>(cv, m - v0);
+      // the previous chunk's permutes must be done before the buffer is reused
+      cudaError_t e = cudaStreamSynchronize(c->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(staging, hsrc + (size_t)(v0 * S) * (cplx ? 2 : 1), elem * nv * S,
+                            kind, c->stream);
+      for (int i = 0; i < p.count && e == cudaSuccess; ++i) {
+        int64_t nb[4], t[4];
+        for (int k = 0; k < 4; ++k) nb[k] = p.n[i][k];
+        t[0] = 1;
+        for (int k = 1; k < 4; ++k) t[k] = t[k - 1] * p.n[i][k - 1];
+        nb[dslow[i]] = nv;
+        double *dst = *p.dst[i] + (size_t)(v0 * t[dslow[i]]) * (cplx ? 2 : 1);
+        e = launch_permute4_box(dst, staging, nb, p.s[i], t, c->stream, cplx);
+      }
+      if (e != cudaSuccess) {
+        set_error(std::string("chunked upload: ") + cudaGetErrorString(e));
+        rc = e == cudaErrorMemoryAllocation ? ATRIP_ERR_OUT_OF_MEMORY : ATRIP_ERR_CUDA;
+      }
+    }
+    cudaStreamSynchronize(c->stream);
+    cudaFree(staging);
+    if (rc != ATRIP_OK) return rc;
   } else {
     PermutePlan p = plan_for(c, tensor);
     const double *colmajor = src;

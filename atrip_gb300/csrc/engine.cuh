@@ -80,6 +80,10 @@ int triples_fp64_batch_max_blocks_per_sm(int max_no, int min_blocks);
 // elements of one double, or of two (re, im) when complex_elems
 cudaError_t launch_permute4(double *dst, const double *src, const int64_t n[4],
                             const int64_t s[4], cudaStream_t st, bool complex_elems);
+// General box: dst[i . t] = src[i . s] over the n0 x n1 x n2 x n3 box.
+cudaError_t launch_permute4_box(double *dst, const double *src, const int64_t n[4],
+                                const int64_t s[4], const int64_t t[4], cudaStream_t st,
+                                bool complex_elems);
 
 // Complex field: the same launch arguments, every tensor pointer holding
 // interleaved (re, im) pairs, workspace 4 No^3 doubles per CTA.

@@ -14,21 +14,26 @@ namespace {
 
 // 4-D permutation as a gather: coalesced stores, strided loads.  Runs once
 // per uploaded tensor.
+// Box n0 x n1 x n2 x n3: dst[i . t] = src[i . s] (strides in elements).
+// With t the packed strides of the box the stores are coalesced.
+struct Box4 {
+  int64_t n[4], s[4], t[4];
+};
+
 template <typename T>
-__global__ void permute4_kernel(T *__restrict__ dst, const T *__restrict__ src,
-                                int64_t n0, int64_t n1, int64_t n2, int64_t n3, int64_t s0,
-                                int64_t s1, int64_t s2, int64_t s3) {
-  const int64_t total = n0 * n1 * n2 * n3;
+__global__ void permute4_kernel(T *__restrict__ dst, const T *__restrict__ src, Box4 b) {
+  const int64_t total = b.n[0] * b.n[1] * b.n[2] * b.n[3];
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     int64_t r = idx;
-    const int64_t i0 = r % n0;
-    r /= n0;
-    const int64_t i1 = r % n1;
-    r /= n1;
-    const int64_t i2 = r % n2;
-    const int64_t i3 = r / n2;
-    dst[idx] = src[i0 * s0 + i1 * s1 + i2 * s2 + i3 * s3];
+    const int64_t i0 = r % b.n[0];
+    r /= b.n[0];
+    const int64_t i1 = r % b.n[1];
+    r /= b.n[1];
+    const int64_t i2 = r % b.n[2];
+    const int64_t i3 = r / b.n[2];
+    dst[i0 * b.t[0] + i1 * b.t[1] + i2 * b.t[2] + i3 * b.t[3]] =
+        src[i0 * b.s[0] + i1 * b.s[1] + i2 * b.s[2] + i3 * b.s[3]];
   }
 }
 
@@ -93,20 +98,31 @@ __global__ void energy_sum_stage2(const double *__restrict__ partials, int nb,
 
 }  // namespace
 
-cudaError_t launch_permute4(double *dst, const double *src, const int64_t n[4], const int64_t s[4],
-                            cudaStream_t st, bool complex_elems) {
+cudaError_t launch_permute4_box(double *dst, const double *src, const int64_t n[4],
+                                const int64_t s[4], const int64_t t[4], cudaStream_t st,
+                                bool complex_elems) {
+  Box4 b;
+  for (int d = 0; d < 4; ++d) {
+    b.n[d] = n[d];
+    b.s[d] = s[d];
+    b.t[d] = t[d];
+  }
   const int64_t total = n[0] * n[1] * n[2] * n[3];
   if (total == 0) return cudaSuccess;
   int64_t blocks = (total + 255) / 256;
   if (blocks > 152 * 64) blocks = 152 * 64;
   if (complex_elems)
     permute4_kernel<double2><<<(int)blocks, 256, 0, st>>>(
-        reinterpret_cast<double2 *>(dst), reinterpret_cast<const double2 *>(src), n[0], n[1],
-        n[2], n[3], s[0], s[1], s[2], s[3]);
+        reinterpret_cast<double2 *>(dst), reinterpret_cast<const double2 *>(src), b);
   else
-    permute4_kernel<double><<<(int)blocks, 256, 0, st>>>(dst, src, n[0], n[1], n[2], n[3], s[0],
-                                                         s[1], s[2], s[3]);
+    permute4_kernel<double><<<(int)blocks, 256, 0, st>>>(dst, src, b);
   return cudaGetLastError();
+}
+
+cudaError_t launch_permute4(double *dst, const double *src, const int64_t n[4], const int64_t s[4],
+                            cudaStream_t st, bool complex_elems) {
+  const int64_t t[4] = {1, n[0], n[0] * n[1], n[0] * n[1] * n[2]};
+  return launch_permute4_box(dst, src, n, s, t, st, complex_elems);
 }
 
 cudaError_t launch_energy_sum(const double *x, const double *y, int64_t n, double *partials,

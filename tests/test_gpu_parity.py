@@ -156,3 +156,35 @@ def test_python_atrip_api_with_checkpoints(tmp_path):
     inp.with_read_checkpoint_if_exists(True).with_checkpoint_at_percentage(10.0)
     out3 = Atrip.run(inp)
     assert _close(out3.energy, e_ref)
+
+
+def test_chunked_host_upload_matches(tmp_path):
+    """Host uploads larger than the staging bound are streamed through a
+    bounded buffer a run of source slices at a time; a tiny bound (set for
+    a child process) gives the same energies as the one-shot upload."""
+    import json
+    import os
+    import subprocess
+    import sys
+    code = (
+        "import json, sys; sys.path.insert(0, %r)\n"
+        "from atrip_gb300 import capi, synth\n"
+        "out = []\n"
+        "for field in ('real', 'complex'):\n"
+        "    d = synth.make_inputs(7, 13, 3, with_j=True, field=field)\n"
+        "    with capi.Context(7, 13, 0, field=field) as c:\n"
+        "        for n in ('epsi','epsa','Tai','Tabij','Vabij','Vijka','Vabci','Jijka','Jabci'):\n"
+        "            c.upload(n, d[n])\n"
+        "        r = c.run(form='fp64')\n"
+        "        out.append([r.energy, r.ct_energy])\n"
+        "print(json.dumps(out))\n" % os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    res = {}
+    for elems in ("", "97"):
+        env = dict(os.environ)
+        env.pop("ATRIP_GB300_STAGING_ELEMS", None)
+        if elems:
+            env["ATRIP_GB300_STAGING_ELEMS"] = elems
+        p = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                           check=True)
+        res[elems] = json.loads(p.stdout.strip().splitlines()[-1])
+    assert res[""] == res["97"], res
