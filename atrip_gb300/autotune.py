@@ -173,10 +173,11 @@ def tune_split(ctx: capi.Context, slices: int, flops: float = 2e13, m: int = 8) 
     n = capi.n_tuples(ctx.Nv)
     wins = windows(n, m, window_size(ctx.No, ctx.Nv, m, flops))
     run_windows(ctx, wins[:1], "split_bf16", slices)  # warm-up (cuts the slices)
-    timed = [(_time(ctx, wins, "split_bf16", slices, {"split_stages": st}), st)
-             for st in (0, 3, 4)]
-    best_ms, st = min(timed, key=lambda x: x[0])
-    tuning = {"split_stages": st}
+    cands = [{"split_stages": st} for st in (0, 3, 4)]
+    if ctx.No <= 24:  # W copy in shared memory, or a deeper ring with W in L2
+        cands += [{"split_stages": st, "split_w_global": 1} for st in (0, 5)]
+    timed = [(_time(ctx, wins, "split_bf16", slices, c), c) for c in cands]
+    best_ms, tuning = min(timed, key=lambda x: x[0])
     ctx.set_tuning(**tuning)
     return {"tuning": tuning, "ms": best_ms, "trials": timed}
 

@@ -15,6 +15,7 @@ struct SplitState {
   void *impl = nullptr;
   uint64_t generation = 0;  // bumped whenever device buffers are (re)allocated
   int stage_cap = 0;        // operand ring depth limit (0 = as many as fit)
+  bool w_global = false;    // energy warps read W from L2 even when it fits in smem
 };
 
 void split_invalidate(SplitState &s);

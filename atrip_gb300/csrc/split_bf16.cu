@@ -647,6 +647,7 @@ struct SplitImpl {
   size_t wglobal_floats = 0;
   int *d_status = nullptr;
   int stage_cap = 0;  // operand ring depth limit (0 = as many as fit)
+  bool w_global = false;
   SplitMaps maps;
 };
 
@@ -909,7 +910,7 @@ template <int S, int NP>
 int launch_np(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   const bool split0 = 2 * (a.Nv + a.No) > 1024;
   // the FP64 copy of W fits next to three operand stages up to No = 24
-  const bool wsmem = a.No <= 24;
+  const bool wsmem = a.No <= 24 && !p->w_global;
   if (wsmem)
     return split0 ? launch_shape<S, NP, true, true>(p, a, sm_count, st)
                   : launch_shape<S, NP, false, true>(p, a, sm_count, st);
@@ -988,6 +989,7 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
     return ATRIP_ERR_STATE;
   }
   p->stage_cap = s.stage_cap;
+  p->w_global = s.w_global;
   ATRIP_CUDA_TRY(cudaMemsetAsync(p->wglobal, 0, sizeof(float) * need, st));
   ATRIP_CUDA_TRY(cudaMemsetAsync(p->d_status, 0, sizeof(int), st));
   SplitArgs a;

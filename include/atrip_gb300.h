@@ -152,7 +152,10 @@ typedef struct {
   int32_t split_ctas;       /* split form: persistent CTAs, <= SMs (0 = one per SM) */
   int32_t fp64_min_blocks;  /* FP64 form: 2 = kernel built for 2 CTAs/SM (<= 128   */
                             /* registers), 0 = register budget left to the compiler */
-  int32_t reserved[2];
+  int32_t split_w_global;   /* split form: 1 = energy warps read W from L2 even   */
+                            /* when its FP64 copy fits in shared memory (No <= 24), */
+                            /* leaving that memory to a deeper operand ring        */
+  int32_t reserved[1];
 } atrip_tuning;
 
 /* Set / read the context's launch parameters (kept until changed). */

@@ -103,3 +103,24 @@ def test_split_rejects_bad_slices():
         assert ei.value.status == capi.ERR_ARGUMENT
         # the FP64 form still works on the same context
         assert np.isfinite(ctx.run(form="fp64").energy)
+
+
+@pytest.mark.parametrize("No,Nv,seed", [(6, 10, 1), (24, 30, 4), (17, 70, 9), (1, 6, 7)])
+def test_split_w_global_and_ring_depth_do_not_change_results(No, Nv, seed):
+    """The autotuner's split knobs (ring depth, W read from L2 instead of
+    its shared-memory copy) change the schedule, not the arithmetic: the
+    per-tuple energies stay the same to FP32-reassociation level."""
+    d = synth.make_inputs(No, Nv, seed, with_j=True)
+    d_noj = {k: v for k, v in d.items() if k not in ("Jijka", "Jabci")}
+    n = min(synth.n_tuples(Nv), 300)
+    with _ctx(d_noj) as ctx:
+        ref = ctx.run(form="split_bf16", slices=3, max_iterations=n - 1)
+        e_ref, _ = ctx.tuple_energies(0, n)
+        for tune in ({"split_w_global": 1}, {"split_w_global": 1, "split_stages": 2},
+                     {"split_stages": 3}):
+            ctx.set_tuning(**tune)
+            r = ctx.run(form="split_bf16", slices=3, max_iterations=n - 1)
+            e, _ = ctx.tuple_energies(0, n)
+            s = np.max(np.abs(e_ref))
+            assert np.max(np.abs(e - e_ref)) <= 1e-12 * s, tune
+            assert abs(r.energy - ref.energy) <= 1e-12 * abs(ref.energy), tune
