@@ -11,7 +11,9 @@ keeps the fastest:
 * split form: the slice count first -- the smallest S in 2..4 whose
   estimated |dE(T)| against the FP64 form, carried to the power-of-two scaled
   twin of the system with |E(T)| ~ 0.1 Eh, stays within ``tol_eh`` -- then
-  the depth of the operand ring.
+  the depth of the operand ring, where W lives (shared memory or L2) and the
+  processing order (list order, or grouped in (a, b, c) blocks of side L so
+  the tuples in flight share their operand slabs in L2).
 
 The error estimate runs both forms on the same windows, evenly spread over
 the list, and extrapolates the per-tuple differences to the whole list
@@ -178,6 +180,14 @@ def tune_split(ctx: capi.Context, slices: int, flops: float = 2e13, m: int = 8) 
         cands += [{"split_stages": st, "split_w_global": 1} for st in (0, 5)]
     timed = [(_time(ctx, wins, "split_bf16", slices, c), c) for c in cands]
     best_ms, tuning = min(timed, key=lambda x: x[0])
+    # then the processing order: tuples grouped by (a, b, c) blocks of side L
+    # keep the slabs of the tuples in flight in L2
+    for L in (4, 6, 8, 12):
+        c = dict(tuning, tuple_block=L)
+        t = _time(ctx, wins, "split_bf16", slices, c)
+        timed.append((t, c))
+        if t < 0.98 * best_ms:
+            best_ms, tuning = t, c
     ctx.set_tuning(**tuning)
     return {"tuning": tuning, "ms": best_ms, "trials": timed}
 

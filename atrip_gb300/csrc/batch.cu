@@ -105,6 +105,7 @@ void fill_table(atrip_gpu_batch *b, int64_t first, int64_t max_it, double tai_si
     a.n_triples = c->n_triples;
     a.t_begin = t_begin;
     a.t_end = t_end;
+    a.order = nullptr;
     a.queue = b->d_queue + 8 * k;
     a.tai_sign = tai_sign;
     a.use_j = (use_j && c->have[ATRIP_JIJKA] && c->have[ATRIP_JABCI]) ? 1 : 0;
@@ -286,7 +287,7 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
           const TriplesArgs &a = b->h_table[k];
           if (a.t_end == a.t_begin) continue;
           int rc2 = split_enqueue(c->split, c->dt, c->No, c->Nv, split_ctas(c), a.tuples,
-                                  a.triples, a.n_triples, a.t_begin, a.t_end, tai_sign,
+                                  a.triples, a.n_triples, a.t_begin, a.t_end, nullptr, tai_sign,
                                   a.use_j != 0, b->d_queue + 8 * k, a.e, a.ect, b->stream,
                                   &launches);
           if (rc2 != ATRIP_OK) return rc2;

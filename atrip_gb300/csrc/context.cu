@@ -29,6 +29,43 @@ int fail(int code, const std::string &msg) {
   return code;
 }
 
+// Processing order of tuples [t_begin, t_end) for block side L >= 2: a
+// stable counting sort of the list positions by the block triple
+// (a/L, b/L, c/L), so that the tuples the persistent CTAs hold at any
+// moment read the slabs of few a, b, c values and find them in L2 (in list
+// order ~150 tuples in flight touch ~150 different c slabs).  Within a block
+// triple the list order is kept.  Writes order[q] = position - t_begin.
+int build_order(atrip_gpu_context *c, int64_t t_begin, int64_t t_end, int L, cudaStream_t st) {
+  if (c->order_lo == t_begin && c->order_hi == t_end && c->order_block == L && c->d_order)
+    return ATRIP_OK;
+  const int64_t n = t_end - t_begin;
+  while (((int64_t)c->Nv + L - 1) / L > 400) ++L;  // at most 400^3 block triples
+  const int64_t nb = (c->Nv + L - 1) / L;
+  std::vector<uint32_t> count((size_t)(nb * nb * nb) + 1, 0), out((size_t)n);
+  auto key = [&](uint32_t pk) {
+    const int64_t a = pk & 0x3ff, b = (pk >> 10) & 0x3ff, cc = (pk >> 20) & 0x3ff;
+    return (size_t)(((a / L) * nb + b / L) * nb + cc / L);
+  };
+  for (int64_t t = t_begin; t < t_end; ++t) count[key(c->h_tuples[(size_t)t]) + 1]++;
+  for (size_t k = 1; k < count.size(); ++k) count[k] += count[k - 1];
+  for (int64_t t = t_begin; t < t_end; ++t)
+    out[count[key(c->h_tuples[(size_t)t])]++] = (uint32_t)(t - t_begin);
+  if (n > c->order_cap) {
+    cudaFree(c->d_order);
+    c->d_order = nullptr;
+    c->order_cap = 0;
+    ATRIP_CUDA_TRY(cudaMalloc(&c->d_order, sizeof(uint32_t) * (size_t)n));
+    c->order_cap = n;
+  }
+  ATRIP_CUDA_TRY(cudaMemcpyAsync(c->d_order, out.data(), sizeof(uint32_t) * (size_t)n,
+                                 cudaMemcpyHostToDevice, st));
+  ATRIP_CUDA_TRY(cudaStreamSynchronize(st));  // out is released on return
+  c->order_lo = t_begin;
+  c->order_hi = t_end;
+  c->order_block = L;
+  return ATRIP_OK;
+}
+
 int64_t expected_elements(const atrip_gpu_context *c, int t) {
   const int64_t No = c->No, Nv = c->Nv;
   switch (t) {
@@ -319,6 +356,7 @@ int atrip_gpu_create(const atrip_dims *dims, atrip_gpu_context **out) {
     CREATE_TRY(cudaMalloc(&c->d_tuples, sizeof(uint32_t) * std::max<size_t>(h.size(), 1)));
     CREATE_TRY(cudaMemcpy(c->d_tuples, h.data(), sizeof(uint32_t) * h.size(),
                           cudaMemcpyHostToDevice));
+    c->h_tuples.swap(h);
   }
   // (i >= j >= k) triples in the loop order of src/atrip/Equations.cxx:111-124
   {
@@ -387,6 +425,12 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
     return fail(ATRIP_ERR_UNSUPPORTED, "complex field: only the FP64 form is built");
   int slices = opts->slices > 0 ? opts->slices : 3;
   int64_t launches = 0;
+  const uint32_t *order = nullptr;
+  if (n > 0 && c->tune.tuple_block > 1) {
+    const int rc = build_order(c, t_begin, t_end, c->tune.tuple_block, st);
+    if (rc != ATRIP_OK) return rc;
+    order = c->d_order;
+  }
   ATRIP_CUDA_TRY(cudaEventRecord(c->ev0, st));
   if (n > 0) {
     ATRIP_CUDA_TRY(cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned long long) * 4, st));
@@ -423,6 +467,7 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
       a.n_triples = c->n_triples;
       a.t_begin = t_begin;
       a.t_end = t_end;
+      a.order = order;
       a.queue = c->d_queue;
       a.tai_sign = opts->ijkabc ? -1.0 : 1.0;
       a.use_j = use_j ? 1 : 0;
@@ -443,7 +488,8 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
       const int ctas = c->tune.split_ctas > 0 ? std::min(c->sm_count, (int)c->tune.split_ctas)
                                               : c->sm_count;
       int rc = split_run(c->split, c->dt, c->No, c->Nv, ctas, c->d_tuples, c->d_triples,
-                         c->n_triples, t_begin, t_end, opts->ijkabc ? -1.0 : 1.0, use_j, slices,
+                         c->n_triples, t_begin, t_end, order, opts->ijkabc ? -1.0 : 1.0, use_j,
+                         slices,
                          c->d_queue, c->d_e, c->d_ect, st, &launches);
       if (rc != ATRIP_OK) return rc;
     }
@@ -482,6 +528,8 @@ int atrip_gpu_set_tuning(atrip_gpu_context *c, const atrip_tuning *t) {
     return fail(ATRIP_ERR_ARGUMENT, "negative tuning value");
   if (t->fp64_tile_rows != 0 && t->fp64_tile_rows != 32 && t->fp64_tile_rows != 64)
     return fail(ATRIP_ERR_ARGUMENT, "fp64_tile_rows must be 32 or 64");
+  if (t->tuple_block < 0 || t->tuple_block > 1023)
+    return fail(ATRIP_ERR_ARGUMENT, "tuple_block must be in [0, 1023]");
   if (t->split_stages != 0 && (t->split_stages < 2 || t->split_stages > 6))
     return fail(ATRIP_ERR_ARGUMENT, "split_stages must be 2..6");
   if (t->tuples_per_claim > 64) return fail(ATRIP_ERR_ARGUMENT, "tuples_per_claim must be <= 64");
@@ -525,6 +573,7 @@ int atrip_gpu_destroy(atrip_gpu_context *c) {
   cudaFree(c->d_queue);
   cudaFree(c->d_partials);
   cudaFree(c->d_sum);
+  cudaFree(c->d_order);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);

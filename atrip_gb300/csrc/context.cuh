@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "atrip_gb300.h"
 #include "engine.cuh"
@@ -29,4 +30,9 @@ struct atrip_gpu_context {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   atrip_gb300::SplitState split;
   atrip_tuning tune = {};
+  // processing order of the last range (tuple_block > 1), see build_order
+  std::vector<uint32_t> h_tuples;  // packed list, host copy
+  uint32_t *d_order = nullptr;
+  int64_t order_cap = 0, order_lo = -1, order_hi = -1;
+  int order_block = 0;
 };

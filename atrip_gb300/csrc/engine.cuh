@@ -45,6 +45,8 @@ struct TriplesArgs {
   const uint32_t *triples;  // packed i | j << 8 | k << 16 with i >= j >= k
   int n_triples;
   int64_t t_begin, t_end;   // tuple-list range of this launch
+  const uint32_t *order;    // processing order: queue slot q runs list position
+                            // t_begin + order[q] (nullptr: t_begin + q)
   unsigned long long *queue;// work-queue cursor (zeroed before launch)
   double tai_sign;          // -1 for ijkabc (src/atrip/Atrip.cxx:183-187)
   int use_j;

@@ -28,8 +28,9 @@ int split_prepare(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
 // captured into a CUDA graph).  The caller zeroes *queue first.
 int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
                   const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,
-                  int64_t t_end, double tai_sign, bool use_j, unsigned long long *queue,
-                  double *e, double *ect, cudaStream_t st, int64_t *launches);
+                  int64_t t_end, const uint32_t *order, double tai_sign, bool use_j,
+                  unsigned long long *queue, double *e, double *ect, cudaStream_t st,
+                  int64_t *launches);
 // Device status word of the last launch (0 = fine) and its host check.
 const int *split_status_ptr(const SplitState &s);
 int split_status_check(int status);
@@ -37,7 +38,7 @@ int split_status_check(int status);
 // Runs tuples [t_begin, t_end) in the split form, writing e[t], ect[t].
 int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
               const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,
-              int64_t t_end, double tai_sign, bool use_j, int slices,
+              int64_t t_end, const uint32_t *order, double tai_sign, bool use_j, int slices,
               unsigned long long *queue, double *e, double *ect, cudaStream_t st,
               int64_t *launches);
 

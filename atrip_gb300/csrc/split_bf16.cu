@@ -80,6 +80,7 @@ struct SplitArgs {
   const uint32_t *tuples, *triples;
   int n_triples;
   int64_t t_begin, t_end;
+  const uint32_t *order;  // queue slot q runs list position t_begin + order[q]
   unsigned long long *queue;
   double tai_sign, unit, unit_j;
   int use_j;  // second pass with the J intermediates ((cT) energy)
@@ -301,7 +302,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const bool stop = !alive || q >= (unsigned long long)(g.t_end - g.t_begin) ||
                           *reinterpret_cast<volatile int *>(g.status) != 0;
         TupleSlot s;
-        s.t = stop ? -1 : g.t_begin + (int64_t)q;
+        s.t = stop ? -1 : g.t_begin + (g.order ? (int64_t)g.order[q] : (int64_t)q);
         s.a = s.b = s.c = 0;
         if (!stop) {
           const uint32_t pk = g.tuples[s.t];
@@ -385,23 +386,26 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (SPLIT0 && pt >= 2 && sa == 0) {
                   // level 0 of the transposed half has its own accumulator
 #pragma unroll
-                  for (int kk = 0; kk < nkk; ++kk)
-                    mma_bf16(dbase + S * NP, adesc + 2 * kk, bdesc + 2 * kk,
-                             idesc_bf16_f32(128, NP), (fresh_tr0 && kk == 0) ? 0u : 1u);
+                  for (int kk = 0; kk < kKChunk / 16; ++kk)
+                    if (kk < nkk)
+                      mma_bf16(dbase + S * NP, adesc + 2 * kk, bdesc + 2 * kk,
+                               idesc_bf16_f32(128, NP), (fresh_tr0 && kk == 0) ? 0u : 1u);
                   fresh_tr0 = false;
                   if (S > 1) {
                     const uint64_t bdesc1 = sdesc_sw128(sbase + kATileBytes + K::kBTile);
 #pragma unroll
-                    for (int kk = 0; kk < nkk; ++kk)
-                      mma_bf16(dbase + NP, adesc + 2 * kk, bdesc1 + 2 * kk,
-                               idesc_bf16_f32(128, (S - 1) * NP), 1u);
+                    for (int kk = 0; kk < kKChunk / 16; ++kk)
+                      if (kk < nkk)
+                        mma_bf16(dbase + NP, adesc + 2 * kk, bdesc1 + 2 * kk,
+                                 idesc_bf16_f32(128, (S - 1) * NP), 1u);
                   }
                 } else {
                   const uint32_t id = idesc_bf16_f32(128, (S - sa) * NP);
 #pragma unroll
-                  for (int kk = 0; kk < nkk; ++kk)
-                    mma_bf16(dbase + sa * NP, adesc + 2 * kk, bdesc + 2 * kk, id,
-                             (fresh_main && kk == 0) ? 0u : 1u);
+                  for (int kk = 0; kk < kKChunk / 16; ++kk)
+                    if (kk < nkk)
+                      mma_bf16(dbase + sa * NP, adesc + 2 * kk, bdesc + 2 * kk, id,
+                               (fresh_main && kk == 0) ? 0u : 1u);
                   fresh_main = false;
                 }
                 mma_commit(&empty[st]);
@@ -976,8 +980,9 @@ int split_prepare(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
 
 int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
                   const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,
-                  int64_t t_end, double tai_sign, bool use_j, unsigned long long *queue,
-                  double *e, double *ect, cudaStream_t st, int64_t *launches) {
+                  int64_t t_end, const uint32_t *order, double tai_sign, bool use_j,
+                  unsigned long long *queue, double *e, double *ect, cudaStream_t st,
+                  int64_t *launches) {
   auto *p = static_cast<SplitImpl *>(s.impl);
   if (!s.valid || !p || (use_j && !p->has_j)) {
     set_error("split form: operands not prepared");
@@ -1007,6 +1012,7 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
   a.n_triples = n_triples;
   a.t_begin = t_begin;
   a.t_end = t_end;
+  a.order = order;
   a.queue = queue;
   a.tai_sign = tai_sign;
   a.unit = p->unit;
@@ -1042,12 +1048,12 @@ int split_status_check(int status) {
 
 int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
               const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,
-              int64_t t_end, double tai_sign, bool use_j, int slices,
+              int64_t t_end, const uint32_t *order, double tai_sign, bool use_j, int slices,
               unsigned long long *queue, double *e, double *ect, cudaStream_t st,
               int64_t *launches) {
   int rc = split_prepare(s, dt, No, Nv, sm_count, use_j, slices, st, launches);
   if (rc != ATRIP_OK) return rc;
-  rc = split_enqueue(s, dt, No, Nv, sm_count, tuples, triples, n_triples, t_begin, t_end,
+  rc = split_enqueue(s, dt, No, Nv, sm_count, tuples, triples, n_triples, t_begin, t_end, order,
                      tai_sign, use_j, queue, e, ect, st, launches);
   if (rc != ATRIP_OK) return rc;
   int status = 0;

@@ -27,7 +27,8 @@ __global__ void __launch_bounds__(kThreads, MINB) triples_fp64_kernel(TriplesArg
     __syncthreads();
     if (slot < 0) break;
     const int64_t last = slot + claim < n ? slot + claim : n;
-    for (int64_t u = slot; u < last; ++u) process_tuple<NC, RU>(g, sm, s, Wv, Wj, g.t_begin + u);
+    for (int64_t u = slot; u < last; ++u)
+      process_tuple<NC, RU>(g, sm, s, Wv, Wj, g.t_begin + (g.order ? (int64_t)g.order[u] : u));
   }
 }
 

@@ -59,6 +59,7 @@ struct ZArgs {
   const uint32_t *tuples, *triples;
   int n_triples;
   int64_t t_begin, t_end;
+  const uint32_t *order;
   unsigned long long *queue;
   double tai_sign;
   int use_j;
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(kThreads) triples_z_kernel(ZArgs g) {
     const long long slot = sm.tuple_slot;
     __syncthreads();
     if (slot < 0) break;
-    const int64_t t = g.t_begin + slot;
+    const int64_t t = g.t_begin + (g.order ? (int64_t)g.order[slot] : (int64_t)slot);
     const uint32_t pk = g.tuples[t];
     const int a = pk & 0x3ff, b = (pk >> 10) & 0x3ff, c = (pk >> 20) & 0x3ff;
     if (threadIdx.x < No) {
@@ -320,6 +321,7 @@ cudaError_t launch_triples_z(const TriplesArgs &ta, int grid, cudaStream_t s) {
   a.n_triples = ta.n_triples;
   a.t_begin = ta.t_begin;
   a.t_end = ta.t_end;
+  a.order = ta.order;
   a.queue = ta.queue;
   a.tai_sign = ta.tai_sign;
   a.use_j = ta.use_j;

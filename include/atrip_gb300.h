@@ -155,7 +155,11 @@ typedef struct {
   int32_t split_w_global;   /* split form: 1 = energy warps read W from L2 even   */
                             /* when its FP64 copy fits in shared memory (No <= 24), */
                             /* leaving that memory to a deeper operand ring        */
-  int32_t reserved[1];
+  int32_t tuple_block;      /* processing order of the run's tuples: 0/1 = list    */
+                            /* order; L >= 2 = grouped by (a/L, b/L, c/L) blocks,  */
+                            /* so the tuples in flight share their a, b, c slabs   */
+                            /* in L2 (results are unchanged: per-tuple energies    */
+                            /* stay indexed by list position)                      */
 } atrip_tuning;
 
 /* Set / read the context's launch parameters (kept until changed). */

@@ -124,3 +124,19 @@ def test_split_w_global_and_ring_depth_do_not_change_results(No, Nv, seed):
             s = np.max(np.abs(e_ref))
             assert np.max(np.abs(e - e_ref)) <= 1e-12 * s, tune
             assert abs(r.energy - ref.energy) <= 1e-12 * abs(ref.energy), tune
+
+
+def test_split_level0_split_accumulator_large_k():
+    """K = 2 (Nv + No) > 1024 (the No=56/Nv=560 workload's regime): level 0
+    of the transposed half gets its own exact accumulator.  Per-tuple
+    energies stay within the 3-slice bound of the FP64 form."""
+    No, Nv = 3, 515
+    d = synth.make_inputs(No, Nv, 11)
+    n = 256
+    with _ctx(d) as ctx:
+        ctx.run(form="fp64", max_iterations=n - 1)
+        e64, _ = ctx.tuple_energies(0, n)
+        ctx.run(form="split_bf16", slices=3, max_iterations=n - 1)
+        es, _ = ctx.tuple_energies(0, n)
+    scale = np.max(np.abs(e64))
+    assert np.max(np.abs(es - e64)) <= BOUND[3] * scale
