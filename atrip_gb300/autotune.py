@@ -178,6 +178,10 @@ def tune_split(ctx: capi.Context, slices: int, flops: float = 2e13, m: int = 8) 
     cands = [{"split_stages": st} for st in (0, 3, 4)]
     if ctx.No <= 24:  # W copy in shared memory, or a deeper ring with W in L2
         cands += [{"split_stages": st, "split_w_global": 1} for st in (0, 5)]
+    if slices * ctx.No <= 128 and 2 * (ctx.Nv + ctx.No) <= 1024:
+        # transposed kernel: stacked slices as M, (p,q) pairs as N <= 256
+        cands += [{"split_variant": 2, "split_stages": st} for st in (0, 3)]
+        cands += [{"split_variant": 2, "split_w_global": 1}]
     timed = [(_time(ctx, wins, "split_bf16", slices, c), c) for c in cands]
     best_ms, tuning = min(timed, key=lambda x: x[0])
     # then the processing order: tuples grouped by (a, b, c) blocks of side L

@@ -16,6 +16,7 @@ struct SplitState {
   uint64_t generation = 0;  // bumped whenever device buffers are (re)allocated
   int stage_cap = 0;        // operand ring depth limit (0 = as many as fit)
   bool w_global = false;    // energy warps read W from L2 even when it fits in smem
+  int variant = 0;          // 2: transposed kernel (stacked slices as M) where eligible
 };
 
 void split_invalidate(SplitState &s);

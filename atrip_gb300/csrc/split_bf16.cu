@@ -43,6 +43,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 #include "engine.cuh"
 #include "sm100.cuh"
@@ -71,10 +72,14 @@ enum : int {
 struct SplitMaps {
   CUtensorMap TaN, TaT, VhN, VhT, Vp, TpN, TpT;
   CUtensorMap JhN, JhT, Jp;  // (cT) intermediates in place of V_hhhp, V_pphp
+  // transposed variant: boxes of jt2 (p,q) row groups for the N side, all S
+  // slices stacked for the M side
+  CUtensorMap TaN2, TaT2, VhN2, VhT2, Vp2, TpN2, TpT2, JhN2, JhT2, Jp2;
 };
 
 struct SplitArgs {
   int No, Nv, jt, ntiles, kch;  // j per M-tile, M-tiles per group, K chunks of Nv
+  int jt2, ntiles2, nmma;       // transposed variant: q per N-tile, N-tiles, MMA N
   int nstages;                 // operand ring depth
   const double *epsi, *epsa, *tai, *Vhh;
   const uint32_t *tuples, *triples;
@@ -137,6 +142,19 @@ __global__ void slice_kernel(SliceJob j) {
 __device__ __forceinline__ void named_bar_sync(int id, int n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
+// Barrier over n threads that also ANDs a predicate across them.
+__device__ __forceinline__ bool named_bar_and(int id, int n, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, %2, %3, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id), "r"(n)
+      : "memory");
+  return r != 0;
+}
 
 struct Part {
   const CUtensorMap *amap, *bmap;
@@ -147,7 +165,7 @@ struct Part {
 // Operand sources of group g, part pt (0 nat particle, 1 nat hole,
 // 2 transposed particle, 3 transposed hole) for tuple (a,b,c).
 __device__ __forceinline__ Part part_of(const SplitMaps &m, int g, int pt, int a, int b, int c,
-                                        int pass) {
+                                        int pass, bool tv) {
   // per group: natural (x, w, (y,z), hole (u,v), holeT), transposed likewise
   int x, w, y, z, u, v, holeT;
   const bool tr = pt >= 2;
@@ -163,16 +181,19 @@ __device__ __forceinline__ Part part_of(const SplitMaps &m, int g, int pt, int a
   }
   Part p;
   p.particle = (pt & 1) == 0;
+  // amap: the (p,q)-row operand (T_x or V_hhhp[w] slab), bmap: the r-column
+  // operand (V_yz or T_uv); tv selects the maps of the transposed variant
   if (p.particle) {
-    p.amap = tr ? &m.TaT : &m.TaN;
+    p.amap = tv ? (tr ? &m.TaT2 : &m.TaN2) : (tr ? &m.TaT : &m.TaN);
     p.ax = x;
-    p.bmap = pass ? &m.Jp : &m.Vp;
+    p.bmap = tv ? (pass ? &m.Jp2 : &m.Vp2) : (pass ? &m.Jp : &m.Vp);
     p.bz = z;
     p.by = y;
   } else {
-    p.amap = pass ? (tr ? &m.JhT : &m.JhN) : (tr ? &m.VhT : &m.VhN);
+    p.amap = tv ? (pass ? (tr ? &m.JhT2 : &m.JhN2) : (tr ? &m.VhT2 : &m.VhN2))
+                : (pass ? (tr ? &m.JhT : &m.JhN) : (tr ? &m.VhT : &m.VhN));
     p.ax = w;
-    p.bmap = holeT ? &m.TpT : &m.TpN;
+    p.bmap = tv ? (holeT ? &m.TpT2 : &m.TpN2) : (holeT ? &m.TpT : &m.TpN);
     p.bz = v;
     p.by = u;
   }
@@ -190,6 +211,25 @@ struct KernelShape {
   static constexpr int kBTile = NP * 128;
   static constexpr int kStageBytes = kATileBytes + S * kBTile;
 };
+
+// Transposed variant: M = 128 rows holding the S slices of the r-column
+// operand stacked (row s No + r), N = nmma <= 256 columns of (p,q) pairs,
+// one 128 x 256 FP32 accumulator per item, double-buffered (all 512 TMEM
+// columns).  Stage: 16 KB M-side tile + 32 KB N-side tile.
+template <int S>
+struct KernelShapeT {
+  static constexpr int kNacc = 1;
+  static constexpr int kBufCols = 256;
+  static constexpr int kNbuf = 2;
+  static constexpr int kCols = 512;
+  static constexpr int kAllocCols = 512;
+  static constexpr int kBTile = 256 * 128;
+  static constexpr int kStageBytes = kATileBytes + kBTile;
+};
+constexpr int kStageCols = 32;   // epilogue staging: 128 rows x 32 FP32 columns,
+constexpr int kStagePitch = 33;  // padded against bank conflicts
+constexpr int kStagingBytes = 128 * kStagePitch * 4;
+constexpr int kMaxRowsPerThread = 16;  // ceil(No / 4) for No <= 64
 
 // Tuple hand-off ring: the producer owns the work queue and publishes each
 // tuple to the MMA issuer, the epilogue warps and the energy warps.
@@ -212,10 +252,10 @@ __device__ __forceinline__ int energy_rank(int warp, int lane) {
 // epilogue warps fill buffer k % 2 for tuple k while the energy warps read
 // buffer (k-1) % 2, so the tensor-core work of one tuple overlaps the FP64
 // energy evaluation of the previous one.
-template <int S, int NP, bool SPLIT0, bool WSMEM>
+template <int S, int NP, bool SPLIT0, bool WSMEM, bool TV>
 __global__ void __launch_bounds__(kThreads, 1)
     triples_split_kernel(const __grid_constant__ SplitMaps maps, const SplitArgs g) {
-  using K = KernelShape<S, NP, SPLIT0>;
+  using K = typename std::conditional<TV, KernelShapeT<S>, KernelShape<S, NP, SPLIT0>>::type;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -243,6 +283,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   double *esm = red + 16;       // eps_i
   double *Vsm = esm + 64;       // 3 No x No blocks for the singles
   double *Wsm = Vsm + 3 * No2;  // FP64 copy of W for the energy loop (WSMEM)
+  float *stg = reinterpret_cast<float *>(Wsm + (WSMEM ? No3 : 0));  // TV epilogue staging
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -285,8 +326,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
-  const int jt = g.jt, ntiles = g.ntiles, kch = g.kch;
-  const int a_bytes = 128 * No * jt;  // full A box, out-of-range rows included
+  const int jt = TV ? g.jt2 : g.jt, ntiles = TV ? g.ntiles2 : g.ntiles, kch = g.kch;
+  const int a_bytes = 128 * No * jt;  // full (p,q)-row box, out-of-range rows included
 
   if (warp == 0) {
     // ------------------------------------------------------ TMA producer
@@ -317,7 +358,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int mt = 0; mt < ntiles && alive; ++mt) {
             const int j0 = mt * jt, grp = gi % 3, pass = gi / 3;
             for (int pt = 0; pt < 4 && alive; ++pt) {
-              const Part p = part_of(maps, grp, pt, s.a, s.b, s.c, pass);
+              const Part p = part_of(maps, grp, pt, s.a, s.b, s.c, pass, TV);
               const int nch = p.particle ? kch : 1;
               for (int ch = 0; ch < nch && alive; ++ch)
                 for (int sa = 0; sa < S; ++sa) {
@@ -328,12 +369,22 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                   }
                   unsigned char *sbase = ring + st * K::kStageBytes;
-                  const int nb = S - sa;
-                  mbar_arrive_expect_tx(&full[st], a_bytes + nb * NP * 128);
-                  tma_load_5d(sbase, p.amap, &full[st], ch * kKChunk, 0, j0, p.ax, sa);
-                  for (int sb = 0; sb < nb; ++sb)
-                    tma_load_5d(sbase + kATileBytes + sb * K::kBTile, p.bmap, &full[st],
-                                ch * kKChunk, 0, p.bz, p.by, sb);
+                  if constexpr (TV) {
+                    // M side: slices -sa .. S-1-sa of the r-column operand
+                    // (those below 0 read as zeros), so row block j always
+                    // holds level j = sa + sb; N side: (p,q) rows, slice sa
+                    mbar_arrive_expect_tx(&full[st], 128 * S * No + a_bytes);
+                    tma_load_5d(sbase, p.bmap, &full[st], ch * kKChunk, 0, p.bz, p.by, -sa);
+                    tma_load_5d(sbase + kATileBytes, p.amap, &full[st], ch * kKChunk, 0, j0, p.ax,
+                                sa);
+                  } else {
+                    const int nb = S - sa;
+                    mbar_arrive_expect_tx(&full[st], a_bytes + nb * NP * 128);
+                    tma_load_5d(sbase, p.amap, &full[st], ch * kKChunk, 0, j0, p.ax, sa);
+                    for (int sb = 0; sb < nb; ++sb)
+                      tma_load_5d(sbase + kATileBytes + sb * K::kBTile, p.bmap, &full[st],
+                                  ch * kKChunk, 0, p.bz, p.by, sb);
+                  }
                   ++unit_count;
                 }
             }
@@ -382,8 +433,17 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint64_t bdesc = sdesc_sw128(sbase + kATileBytes);
                 // A slice sa against B slices 0 .. S-1-sa in one MMA: the
                 // result columns are the level accumulators sa .. S-1, which
-                // sit side by side in TMEM.
-                if (SPLIT0 && pt >= 2 && sa == 0) {
+                // sit side by side in TMEM.  (Transposed variant: the stacked
+                // slices are the M rows, the (p,q) pairs the N columns.)
+                if constexpr (TV) {
+                  const uint32_t id = idesc_bf16_f32(128, g.nmma);
+#pragma unroll
+                  for (int kk = 0; kk < kKChunk / 16; ++kk)
+                    if (kk < nkk)
+                      mma_bf16(dbase, adesc + 2 * kk, bdesc + 2 * kk, id,
+                               (fresh_main && kk == 0) ? 0u : 1u);
+                  fresh_main = false;
+                } else if (SPLIT0 && pt >= 2 && sa == 0) {
                   // level 0 of the transposed half has its own accumulator
 #pragma unroll
                   for (int kk = 0; kk < kKChunk / 16; ++kk)
@@ -431,7 +491,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int ts = k % kTupleSlots;
       bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull);
       const int64_t t = tslot[ts].t;
-      named_bar_sync(1, 128);
+      // agree on ok so that every epilogue thread leaves (or stays) together
+      ok = named_bar_and(1, 128, ok);
       if (threadIdx.x == 128) mbar_arrive(&tempty[ts]);
       if (!ok || t < 0) break;
       const int wb = k & 1;
@@ -448,52 +509,113 @@ __global__ void __launch_bounds__(kThreads, 1)
         okw = __all_sync(0xffffffffu, okw);
         if (!okw) alive = false;
         tc_fence_after();
-        const int j0 = mt * jt;
-        const int rows = No * min(jt, No - j0);
-        const bool valid = l < rows;
-        const int f = l % No, sl = j0 + l / No;
-        const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + buf * K::kBufCols;
-        for (int c0 = 0; c0 < NP && okw; c0 += 16) {
-          float v[K::kNacc][16];
+        if constexpr (TV) {
+          // accumulator: lane s No + r = level s of column r, TMEM column n
+          // = (p,q) pair p + No (q - q0); the four warps stage 32 columns at
+          // a time in shared memory, then each thread recombines the levels
+          // of its (r, column) cells and adds them into W
+          const bool okall = named_bar_and(3, 128, okw);
+          if (!okall) alive = false;
+          const int q0 = mt * jt;
+          const int nvalid = No * min(jt, No - q0);
+          const int t128 = threadIdx.x - 128, cc = t128 & 31, rq = t128 >> 5;
+          const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + buf * K::kBufCols;
+          for (int c0 = 0; c0 < nvalid && okall; c0 += kStageCols) {
+            float v0[16], v1[16];
+            tmem_ld16(tbase + c0, v0);
+            tmem_ld16(tbase + c0 + 16, v1);
+            tmem_wait_ld();
+            float *row = stg + l * kStagePitch;
 #pragma unroll
-          for (int q = 0; q < K::kNacc; ++q) tmem_ld16(tbase + q * NP + c0, v[q]);
-          tmem_wait_ld();
-          if (valid) {
-            // level-0 integer and weighted rest of the 16 columns
-            int lev0[16];
-            float rest[16];
-#pragma unroll
-            for (int cc = 0; cc < 16; ++cc) {
-              lev0[cc] = __float2int_rn(v[0][cc]);
-              if (SPLIT0) lev0[cc] += __float2int_rn(v[S][cc]);
-              float r = 0.f;
-#pragma unroll
-              for (int q = S - 1; q >= 1; --q) r = r * (1.f / 256.f) + v[q][cc];
-              rest[cc] = r * (1.f / 256.f);
+            for (int x = 0; x < 16; ++x) {
+              row[x] = v0[x];
+              row[16 + x] = v1[x];
             }
-            // the 16 cells are distinct elements of W: issue every load
-            // before any store so the round trips to L2 overlap
-            int idx[16];
-            int2 cell[16];
+            named_bar_sync(1, 128);
+            const int n = c0 + cc;
+            int idx[kMaxRowsPerThread];
+            int lev0[kMaxRowsPerThread];
+            float rest[kMaxRowsPerThread];
+            int2 cell[kMaxRowsPerThread];
 #pragma unroll
-            for (int cc = 0; cc < 16; ++cc) {
-              const int col = c0 + cc;
-              int i, jj, kx;
-              if (grp == 0) { i = f; jj = sl; kx = col; }
-              else if (grp == 1) { i = f; kx = sl; jj = col; }
-              else { jj = f; kx = sl; i = col; }
-              idx[cc] = col < No ? i + No * (jj + No * kx) : -1;
-            }
+            for (int u = 0; u < kMaxRowsPerThread; ++u) {
+              const int r = rq + 4 * u;
+              idx[u] = -1;
+              if (r < No && n < nvalid) {
+                lev0[u] = __float2int_rn(stg[r * kStagePitch + cc]);
+                float rr = 0.f;
 #pragma unroll
-            for (int cc = 0; cc < 16; ++cc)
-              if (idx[cc] >= 0) cell[cc] = __ldcg(&Wc[idx[cc]]);
-#pragma unroll
-            for (int cc = 0; cc < 16; ++cc)
-              if (idx[cc] >= 0) {
-                cell[cc].x += lev0[cc];
-                cell[cc].y = __float_as_int(__int_as_float(cell[cc].y) + rest[cc]);
-                __stcg(&Wc[idx[cc]], cell[cc]);
+                for (int q = S - 1; q >= 1; --q)
+                  rr = rr * (1.f / 256.f) + stg[(q * No + r) * kStagePitch + cc];
+                rest[u] = rr * (1.f / 256.f);
+                const int f = n % No, sl = q0 + n / No;
+                int i, jj, kx;
+                if (grp == 0) { i = f; jj = sl; kx = r; }
+                else if (grp == 1) { i = f; kx = sl; jj = r; }
+                else { jj = f; kx = sl; i = r; }
+                idx[u] = i + No * (jj + No * kx);
               }
+            }
+#pragma unroll
+            for (int u = 0; u < kMaxRowsPerThread; ++u)
+              if (idx[u] >= 0) cell[u] = __ldcg(&Wc[idx[u]]);
+#pragma unroll
+            for (int u = 0; u < kMaxRowsPerThread; ++u)
+              if (idx[u] >= 0) {
+                cell[u].x += lev0[u];
+                cell[u].y = __float_as_int(__int_as_float(cell[u].y) + rest[u]);
+                __stcg(&Wc[idx[u]], cell[u]);
+              }
+            named_bar_sync(1, 128);  // the staging buffer is reused
+          }
+        } else {
+          const int j0 = mt * jt;
+          const int rows = No * min(jt, No - j0);
+          const bool valid = l < rows;
+          const int f = l % No, sl = j0 + l / No;
+          const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + buf * K::kBufCols;
+          for (int c0 = 0; c0 < NP && okw; c0 += 16) {
+            float v[K::kNacc][16];
+  #pragma unroll
+            for (int q = 0; q < K::kNacc; ++q) tmem_ld16(tbase + q * NP + c0, v[q]);
+            tmem_wait_ld();
+            if (valid) {
+              // level-0 integer and weighted rest of the 16 columns
+              int lev0[16];
+              float rest[16];
+  #pragma unroll
+              for (int cc = 0; cc < 16; ++cc) {
+                lev0[cc] = __float2int_rn(v[0][cc]);
+                if (SPLIT0) lev0[cc] += __float2int_rn(v[S][cc]);
+                float r = 0.f;
+  #pragma unroll
+                for (int q = S - 1; q >= 1; --q) r = r * (1.f / 256.f) + v[q][cc];
+                rest[cc] = r * (1.f / 256.f);
+              }
+              // the 16 cells are distinct elements of W: issue every load
+              // before any store so the round trips to L2 overlap
+              int idx[16];
+              int2 cell[16];
+  #pragma unroll
+              for (int cc = 0; cc < 16; ++cc) {
+                const int col = c0 + cc;
+                int i, jj, kx;
+                if (grp == 0) { i = f; jj = sl; kx = col; }
+                else if (grp == 1) { i = f; kx = sl; jj = col; }
+                else { jj = f; kx = sl; i = col; }
+                idx[cc] = col < No ? i + No * (jj + No * kx) : -1;
+              }
+  #pragma unroll
+              for (int cc = 0; cc < 16; ++cc)
+                if (idx[cc] >= 0) cell[cc] = __ldcg(&Wc[idx[cc]]);
+  #pragma unroll
+              for (int cc = 0; cc < 16; ++cc)
+                if (idx[cc] >= 0) {
+                  cell[cc].x += lev0[cc];
+                  cell[cc].y = __float_as_int(__int_as_float(cell[cc].y) + rest[cc]);
+                  __stcg(&Wc[idx[cc]], cell[cc]);
+                }
+            }
           }
         }
         tc_fence_before();
@@ -515,7 +637,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int ts = k % kTupleSlots;
       bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull);
       const TupleSlot s = tslot[ts];
-      named_bar_sync(2, kEnergyThreads);
+      ok = named_bar_and(2, kEnergyThreads, ok);  // leave together
       if (er == 0) mbar_arrive(&tempty[ts]);
       if (!ok || s.t < 0) break;
       const int a = s.a, b = s.b, c = s.c;
@@ -652,6 +774,7 @@ struct SplitImpl {
   int *d_status = nullptr;
   int stage_cap = 0;  // operand ring depth limit (0 = as many as fit)
   bool w_global = false;
+  int variant = 0;    // 2: transposed kernel where eligible
   SplitMaps maps;
 };
 
@@ -828,9 +951,38 @@ int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, cudaSt
     if ((rc = make_map(&p->maps.TpN, p->TpS, d, box))) return rc;
     if ((rc = make_map(&p->maps.TpT, p->TpTS, d, box))) return rc;
   }
+  // transposed variant: (p,q)-row boxes of jt2 row groups, r-column boxes
+  // of all S slices (loaded from slice -sa, the rows below 0 read as zeros)
+  const int jt2 = 256 / No;
+  {
+    const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt2, 1, 1};
+    if ((rc = make_map(&p->maps.TaN2, p->TaS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.TaT2, p->TaST, d, box))) return rc;
+  }
+  {
+    const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt2, 1, 1};
+    if ((rc = make_map(&p->maps.VhN2, p->VhS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.VhT2, p->VhST, d, box))) return rc;
+  }
+  {
+    const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)S};
+    if ((rc = make_map(&p->maps.Vp2, p->VpS, d, box))) return rc;
+  }
+  {
+    const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)S};
+    if ((rc = make_map(&p->maps.TpN2, p->TpS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.TpT2, p->TpTS, d, box))) return rc;
+  }
   p->maps.JhN = p->maps.VhN;
   p->maps.JhT = p->maps.VhT;
   p->maps.Jp = p->maps.Vp;
+  p->maps.JhN2 = p->maps.VhN2;
+  p->maps.JhT2 = p->maps.VhT2;
+  p->maps.Jp2 = p->maps.Vp2;
   return ATRIP_OK;
 }
 
@@ -880,6 +1032,18 @@ int prepare_j(SplitImpl *p, const DeviceTensors &dt, cudaStream_t st, int64_t *l
     const uint32_t box[5] = {kKChunk, (uint32_t)NP, 1, 1, 1};
     if ((rc = make_map(&p->maps.Jp, p->JpS, d, box))) return rc;
   }
+  const int jt2 = 256 / No;
+  {
+    const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt2, 1, 1};
+    if ((rc = make_map(&p->maps.JhN2, p->JhS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.JhT2, p->JhST, d, box))) return rc;
+  }
+  {
+    const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)S};
+    if ((rc = make_map(&p->maps.Jp2, p->JpS, d, box))) return rc;
+  }
   p->has_j = true;
   return ATRIP_OK;
 }
@@ -900,7 +1064,7 @@ int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st
   SplitArgs args = a;
   args.nstages = nst;
   const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
-  auto kern = triples_split_kernel<S, NP, SPLIT0, WSMEM>;
+  auto kern = triples_split_kernel<S, NP, SPLIT0, WSMEM, false>;
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   const int64_t n = a.t_end - a.t_begin;
@@ -922,8 +1086,54 @@ int launch_np(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
                 : launch_shape<S, NP, false, false>(p, a, sm_count, st);
 }
 
+// Transposed variant (S No <= 128, K = 2 (Nv + No) <= 1024).  The FP64 copy
+// of W goes to shared memory when at least three operand stages still fit.
+template <int S, bool WSMEM>
+int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
+  using K = KernelShapeT<S>;
+  const size_t No3 = (size_t)a.No * a.No * a.No;
+  const size_t vbytes =
+      sizeof(double) * (3 * (size_t)a.No * a.No + (WSMEM ? No3 : 0)) + kStagingBytes;
+  const size_t avail = kSmemLimit - 1024 - kTailBytes - vbytes;
+  int nst = (int)(avail / K::kStageBytes);
+  if (nst > kMaxStages) nst = kMaxStages;
+  if (p->stage_cap >= 2 && nst > p->stage_cap) nst = p->stage_cap;
+  if (nst < 2) {
+    set_error("split form (transposed): shared memory too small for No=" + std::to_string(a.No));
+    return ATRIP_ERR_UNSUPPORTED;
+  }
+  SplitArgs args = a;
+  args.nstages = nst;
+  const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
+  auto kern = triples_split_kernel<S, 16, false, WSMEM, true>;
+  ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  const int64_t n = a.t_end - a.t_begin;
+  const int grid = (int)(n < sm_count ? n : sm_count);
+  kern<<<grid, kThreads, smem, st>>>(p->maps, args);
+  ATRIP_CUDA_TRY(cudaGetLastError());
+  return ATRIP_OK;
+}
+
+bool transposed_eligible(int S, int No, int Nv) {
+  return S * No <= 128 && 2 * (Nv + No) <= 1024;
+}
+
+template <int S>
+int launch_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
+  const size_t No3 = (size_t)a.No * a.No * a.No;
+  const size_t fixed = 1024 + kTailBytes + kStagingBytes + sizeof(double) * 3 * a.No * a.No;
+  const bool wsmem =
+      !p->w_global && fixed + sizeof(double) * No3 + 3 * KernelShapeT<S>::kStageBytes <=
+                          (size_t)kSmemLimit;
+  return wsmem ? launch_shape_t<S, true>(p, a, sm_count, st)
+               : launch_shape_t<S, false>(p, a, sm_count, st);
+}
+
 template <int S>
 int launch_s(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
+  if (p->variant == 2 && transposed_eligible(S, a.No, a.Nv))
+    return launch_t<S>(p, a, sm_count, st);
   const int No = a.No;
   if (No <= 16) return launch_np<S, 16>(p, a, sm_count, st);
   if (No <= 32) return launch_np<S, 32>(p, a, sm_count, st);
@@ -995,6 +1205,7 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
   }
   p->stage_cap = s.stage_cap;
   p->w_global = s.w_global;
+  p->variant = s.variant;
   ATRIP_CUDA_TRY(cudaMemsetAsync(p->wglobal, 0, sizeof(float) * need, st));
   ATRIP_CUDA_TRY(cudaMemsetAsync(p->d_status, 0, sizeof(int), st));
   SplitArgs a;
@@ -1002,6 +1213,9 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
   a.Nv = Nv;
   a.jt = 128 / No;
   a.ntiles = (No + a.jt - 1) / a.jt;
+  a.jt2 = 256 / No;
+  a.ntiles2 = (No + a.jt2 - 1) / a.jt2;
+  a.nmma = (No * a.jt2 + 15) / 16 * 16;
   a.kch = p->Ep / kKChunk;
   a.epsi = dt.epsi;
   a.epsa = dt.epsa;

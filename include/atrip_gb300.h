@@ -160,6 +160,10 @@ typedef struct {
                             /* so the tuples in flight share their a, b, c slabs   */
                             /* in L2 (results are unchanged: per-tuple energies    */
                             /* stay indexed by list position)                      */
+  int32_t split_variant;    /* split form kernel: 0/1 = M tiles of (p,q) rows;     */
+                            /* 2 = transposed (the S slices of V stacked as the    */
+                            /* M rows, up to 256 (p,q) pairs as N) where S No <=   */
+                            /* 128 and 2 (Nv + No) <= 1024, else variant 1          */
 } atrip_tuning;
 
 /* Set / read the context's launch parameters (kept until changed). */

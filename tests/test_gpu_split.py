@@ -33,13 +33,17 @@ CASES = [(6, 10, 1), (8, 40, 0), (5, 9, 3), (13, 17, 2), (24, 30, 4), (30, 14, 5
 
 @pytest.mark.parametrize("No,Nv,seed", CASES)
 @pytest.mark.parametrize("S", [2, 3, 4])
-def test_split_matches_model_and_fp64(No, Nv, seed, S):
+@pytest.mark.parametrize("variant", [1, 2])
+def test_split_matches_model_and_fp64(No, Nv, seed, S, variant):
+    """variant 2 = the transposed kernel (stacked slices as the MMA's M rows)
+    where S No <= 128; elsewhere it falls back to variant 1."""
     d = synth.make_inputs(No, Nv, seed)
     n = min(synth.n_tuples(Nv), 120)
     model = split_model.split_tuple_energies(d, S, 0, n)
     with _ctx(d) as ctx:
         r64 = ctx.run(form="fp64", use_j=False, max_iterations=n - 1)
         e64, _ = ctx.tuple_energies(0, n)
+        ctx.set_tuning(split_variant=variant)
         r = ctx.run(form="split_bf16", slices=S, use_j=False, max_iterations=n - 1)
         assert r.form_used == capi.FORM_SPLIT_BF16 and r.slices_used == S
         e, ect = ctx.tuple_energies(0, n)
@@ -146,3 +150,27 @@ def test_split_level0_split_accumulator_large_k():
             err[S] = np.max(np.abs(es - e64)) / scale
     assert err[3] <= 1e-5 and err[4] <= 1e-7, err
     assert err[4] < err[3] / 20, err
+
+
+@pytest.mark.parametrize("No,Nv,seed,S", [(5, 9, 3, 3), (24, 30, 4, 3), (40, 12, 2, 3),
+                                          (32, 20, 6, 4), (64, 7, 1, 2), (13, 17, 2, 2)])
+def test_transposed_variant_with_j_and_knobs(No, Nv, seed, S):
+    """The transposed kernel gives the same per-tuple E(T) and E(cT) as the
+    M-tile kernel up to FP32 reassociation of the level >= 1 sums, with the
+    (cT) pass, W in L2 or shared memory and a shallow ring."""
+    d = synth.make_inputs(No, Nv, seed, with_j=True)
+    n = min(synth.n_tuples(Nv), 400)
+    with _ctx(d) as ctx:
+        for name in ("Jijka", "Jabci"):
+            ctx.upload(name, d[name])
+        ctx.set_tuning(split_variant=1)
+        ctx.run(form="split_bf16", slices=S, use_j=True, max_iterations=n - 1)
+        e1, c1 = ctx.tuple_energies(0, n)
+        for tune in ({"split_variant": 2}, {"split_variant": 2, "split_w_global": 1},
+                     {"split_variant": 2, "split_stages": 2, "tuple_block": 4}):
+            ctx.set_tuning(**tune)
+            ctx.run(form="split_bf16", slices=S, use_j=True, max_iterations=n - 1)
+            e2, c2 = ctx.tuple_energies(0, n)
+            s = np.max(np.abs(e1))
+            assert np.max(np.abs(e2 - e1)) <= 1e-9 * s, (tune, np.max(np.abs(e2 - e1)) / s)
+            assert np.max(np.abs(c2 - c1)) <= 1e-9 * s, tune
