@@ -339,7 +339,10 @@ def run_single(args, workload, world, rank, local):
     ctx = capi.Context(No, Nv, local)
     _upload_all(ctx, d)
     stream = torch.cuda.Stream()
-    if args.no_tune:
+    if args.tuning:
+        ctx.set_tuning(**json.loads(args.tuning))
+        tune = {"tuning": ctx.get_tuning(), "slices": args.slices or 3}
+    elif args.no_tune:
         tune = {"tuning": ctx.get_tuning(), "slices": args.slices or 3}
     else:
         tune = autotune.tune(ctx, form, tol_eh=args.tol_eh, use_cache=not args.retune,
@@ -569,6 +572,9 @@ def main():
     ap.add_argument("--retune", action="store_true", help="ignore the tuning cache")
     ap.add_argument("--no-tune", action="store_true",
                     help="built-in launch parameters, --slices or 3 slices (profiling runs)")
+    ap.add_argument("--tuning", default="",
+                    help="explicit atrip_tuning fields as JSON instead of the autotuner "
+                         "(profiling runs), e.g. '{\"split_variant\": 2}'")
     ap.add_argument("--batch-tuples", type=int, default=0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-flops", type=float, default=1e12)
