@@ -80,7 +80,6 @@ struct SplitMaps {
 struct SplitArgs {
   int No, Nv, jt, ntiles, kch;  // j per M-tile, M-tiles per group, K chunks of Nv
   int jt2, ntiles2, nmma;       // transposed variant: q per N-tile, N-tiles, MMA N
-  int vglobal;                  // 1: singles V blocks read from L2, not copied to smem
   int nstages;                 // operand ring depth
   const double *epsi, *epsa, *tai, *Vhh;
   const uint32_t *tuples, *triples;
@@ -283,7 +282,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   double *red = tc + 64;        // [kEnergyWarps]
   double *esm = red + 16;       // eps_i
   double *Vsm = esm + 64;       // 3 No x No blocks for the singles
-  double *Wsm = Vsm + (g.vglobal ? 0 : 3 * No2);  // FP64 copy of W (WSMEM)
+  double *Wsm = Vsm + 3 * No2;  // FP64 copy of W for the energy loop (WSMEM)
   float *stg = reinterpret_cast<float *>(Wsm + (WSMEM ? No3 : 0));  // TV epilogue staging
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -651,12 +650,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         const double *Vbc = g.Vhh + ((int64_t)b * Nv + c) * No2;
         const double *Vac = g.Vhh + ((int64_t)a * Nv + c) * No2;
         const double *Vab = g.Vhh + ((int64_t)a * Nv + b) * No2;
-        if (!g.vglobal)
-          for (int i = er; i < No2; i += kEnergyThreads) {
-            Vsm[i] = Vbc[i];
-            Vsm[No2 + i] = Vac[i];
-            Vsm[2 * No2 + i] = Vab[i];
-          }
+        for (int i = er; i < No2; i += kEnergyThreads) {
+          Vsm[i] = Vbc[i];
+          Vsm[No2 + i] = Vac[i];
+          Vsm[2 * No2 + i] = Vab[i];
+        }
       }
       if (er < No) esm[er] = g.epsi[er];
       const int wb = k & 1;
@@ -682,9 +680,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (b == c) cls--;
       const bool distinct = cls == 0;
       const double epsabc = g.epsa[a] + g.epsa[b] + g.epsa[c];
-      const double *Vbc = g.vglobal ? g.Vhh + ((int64_t)b * Nv + c) * No2 : Vsm;
-      const double *Vac = g.vglobal ? g.Vhh + ((int64_t)a * Nv + c) * No2 : Vsm + No2;
-      const double *Vab = g.vglobal ? g.Vhh + ((int64_t)a * Nv + b) * No2 : Vsm + 2 * No2;
+      const double *Vbc = Vsm, *Vac = Vsm + No2, *Vab = Vsm + 2 * No2;
       auto W = [&](int i, int j, int kx) { return Wd[i + No * (j + No * kx)]; };
       auto Zv = [&](int i, int j, int kx) {
         double z = W(i, j, kx);
@@ -1067,7 +1063,6 @@ int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st
   }
   SplitArgs args = a;
   args.nstages = nst;
-  args.vglobal = 0;
   const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
   auto kern = triples_split_kernel<S, NP, SPLIT0, WSMEM, false>;
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1097,12 +1092,8 @@ template <int S, bool WSMEM>
 int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   using K = KernelShapeT<S>;
   const size_t No3 = (size_t)a.No * a.No * a.No;
-  // above No = 24 the singles blocks (3 No^2 doubles) are read from L2 so
-  // that a fourth 48 KB operand stage fits
-  const int vglobal = a.No > 24 ? 1 : 0;
   const size_t vbytes =
-      sizeof(double) * ((vglobal ? 0 : 3 * (size_t)a.No * a.No) + (WSMEM ? No3 : 0)) +
-      kStagingBytes;
+      sizeof(double) * (3 * (size_t)a.No * a.No + (WSMEM ? No3 : 0)) + kStagingBytes;
   const size_t avail = kSmemLimit - 1024 - kTailBytes - vbytes;
   int nst = (int)(avail / K::kStageBytes);
   if (nst > kMaxStages) nst = kMaxStages;
@@ -1113,7 +1104,6 @@ int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t 
   }
   SplitArgs args = a;
   args.nstages = nst;
-  args.vglobal = vglobal;
   const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
   auto kern = triples_split_kernel<S, 16, false, WSMEM, true>;
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1132,8 +1122,7 @@ bool transposed_eligible(int S, int No, int Nv) {
 template <int S>
 int launch_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   const size_t No3 = (size_t)a.No * a.No * a.No;
-  const size_t fixed = 1024 + kTailBytes + kStagingBytes +
-                       (a.No > 24 ? 0 : sizeof(double) * 3 * a.No * a.No);
+  const size_t fixed = 1024 + kTailBytes + kStagingBytes + sizeof(double) * 3 * a.No * a.No;
   const bool wsmem =
       !p->w_global && fixed + sizeof(double) * No3 + 3 * KernelShapeT<S>::kStageBytes <=
                           (size_t)kSmemLimit;
