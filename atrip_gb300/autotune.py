@@ -184,6 +184,12 @@ def tune_split(ctx: capi.Context, slices: int, flops: float = 2e13, m: int = 8) 
         cands += [{"split_variant": 2, "split_w_global": 1}]
     timed = [(_time(ctx, wins, "split_bf16", slices, c), c) for c in cands]
     best_ms, tuning = min(timed, key=lambda x: x[0])
+    # L2 prefetch of the next part's slab tiles
+    c = dict(tuning, split_prefetch=1)
+    t = _time(ctx, wins, "split_bf16", slices, c)
+    timed.append((t, c))
+    if t < 0.98 * best_ms:
+        best_ms, tuning = t, c
     # then the processing order: tuples grouped by (a, b, c) blocks of side L
     # keep the slabs of the tuples in flight in L2
     for L in (4, 6, 8, 12):

@@ -239,6 +239,7 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
       c->split.stage_cap = c->tune.split_stages;
       c->split.w_global = c->tune.split_w_global != 0;
       c->split.variant = c->tune.split_variant;
+      c->split.prefetch = c->tune.split_prefetch != 0;
       int rc = split_prepare(c->split, c->dt, c->No, c->Nv, split_ctas(c), a.use_j != 0, slices,
                              st, &prep_launches);
       if (rc != ATRIP_OK) return rc;
@@ -249,6 +250,7 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
                                 (uintptr_t)a.t_begin, (uintptr_t)a.t_end,
                                 (uintptr_t)opts->ijkabc, (uintptr_t)c->split.stage_cap,
                                 (uintptr_t)c->split.w_global, (uintptr_t)c->split.variant,
+                                (uintptr_t)c->split.prefetch,
                                 (uintptr_t)split_ctas(c)};
       key.insert(key.end(), std::begin(more), std::end(more));
     }

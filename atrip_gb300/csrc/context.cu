@@ -486,6 +486,7 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
       c->split.stage_cap = c->tune.split_stages;
       c->split.w_global = c->tune.split_w_global != 0;
       c->split.variant = c->tune.split_variant;
+      c->split.prefetch = c->tune.split_prefetch != 0;
       const int ctas = c->tune.split_ctas > 0 ? std::min(c->sm_count, (int)c->tune.split_ctas)
                                               : c->sm_count;
       int rc = split_run(c->split, c->dt, c->No, c->Nv, ctas, c->d_tuples, c->d_triples,

@@ -17,6 +17,7 @@ struct SplitState {
   int stage_cap = 0;        // operand ring depth limit (0 = as many as fit)
   bool w_global = false;    // energy warps read W from L2 even when it fits in smem
   int variant = 0;          // 2: transposed kernel (stacked slices as M) where eligible
+  bool prefetch = false;    // L2 prefetch of the next part's slab tiles
 };
 
 void split_invalidate(SplitState &s);

@@ -80,6 +80,7 @@ struct SplitMaps {
 struct SplitArgs {
   int No, Nv, jt, ntiles, kch;  // j per M-tile, M-tiles per group, K chunks of Nv
   int jt2, ntiles2, nmma;       // transposed variant: q per N-tile, N-tiles, MMA N
+  int prefetch;                 // 1: L2 prefetch of the next part's (p,q)-row tiles
   int nstages;                 // operand ring depth
   const double *epsi, *epsa, *tai, *Vhh;
   const uint32_t *tuples, *triples;
@@ -360,6 +361,21 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int pt = 0; pt < 4 && alive; ++pt) {
               const Part p = part_of(maps, grp, pt, s.a, s.b, s.c, pass, TV);
               const int nch = p.particle ? kch : 1;
+              if (g.prefetch) {
+                // the next part of this tuple: its (p,q)-row tiles (the
+                // slabs of T and V_hhhp, the large operands) into L2 while
+                // this part streams; only boxes wholly inside the tensor
+                int ngi = gi, nmt = mt, npt = pt + 1;
+                if (npt == 4) { npt = 0; if (++nmt == ntiles) { nmt = 0; ++ngi; } }
+                const int nj0 = nmt * jt;
+                if (ngi < 3 * npass && nj0 + jt <= No) {
+                  const Part np = part_of(maps, ngi % 3, npt, s.a, s.b, s.c, ngi / 3, TV);
+                  const int nnch = np.particle ? kch : 1;
+                  for (int ch = 0; ch < nnch; ++ch)
+                    for (int sa = 0; sa < S; ++sa)
+                      tma_prefetch_5d(np.amap, ch * kKChunk, 0, nj0, np.ax, sa);
+                }
+              }
               for (int ch = 0; ch < nch && alive; ++ch)
                 for (int sa = 0; sa < S; ++sa) {
                   const int st = unit_count % kStages;
@@ -1213,6 +1229,7 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
   a.Nv = Nv;
   a.jt = 128 / No;
   a.ntiles = (No + a.jt - 1) / a.jt;
+  a.prefetch = s.prefetch ? 1 : 0;
   a.jt2 = 256 / No;
   a.ntiles2 = (No + a.jt2 - 1) / a.jt2;
   a.nmma = (No * a.jt2 + 15) / 16 * 16;

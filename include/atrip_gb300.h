@@ -164,6 +164,8 @@ typedef struct {
                             /* 2 = transposed (the S slices of V stacked as the    */
                             /* M rows, up to 256 (p,q) pairs as N) where S No <=   */
                             /* 128 and 2 (Nv + No) <= 1024, else variant 1          */
+  int32_t split_prefetch;   /* split form: 1 = prefetch the next part's T / V_hhhp  */
+                            /* slab tiles into L2 while the current part streams   */
 } atrip_tuning;
 
 /* Set / read the context's launch parameters (kept until changed). */

@@ -167,7 +167,9 @@ def test_transposed_variant_with_j_and_knobs(No, Nv, seed, S):
         ctx.run(form="split_bf16", slices=S, use_j=True, max_iterations=n - 1)
         e1, c1 = ctx.tuple_energies(0, n)
         for tune in ({"split_variant": 2}, {"split_variant": 2, "split_w_global": 1},
-                     {"split_variant": 2, "split_stages": 2, "tuple_block": 4}):
+                     {"split_variant": 2, "split_stages": 2, "tuple_block": 4},
+                     {"split_variant": 2, "split_prefetch": 1},
+                     {"split_variant": 1, "split_prefetch": 1}):
             ctx.set_tuning(**tune)
             ctx.run(form="split_bf16", slices=S, use_j=True, max_iterations=n - 1)
             e2, c2 = ctx.tuple_energies(0, n)
