@@ -210,10 +210,12 @@ def run_reference_arm(args, workload):
         sizes = synth.multi_system_sizes(96)[::12]
         systems = [synth.make_inputs(No, Nv, s) for No, Nv, s in sizes]
         desc = "every 12th system of the 96-system workload"
+        wl = ("96 CCSD(T) triples systems, No in [4,20], Nv in [30,200], seeds 0..95")
     else:
         No, Nv = WORKLOADS[workload] if workload in WORKLOADS else (args.no, args.nv)
         systems = [synth.make_inputs(No, Nv, SEED)]
         desc = f"No={No} Nv={Nv} seed {SEED}"
+        wl = f"CCSD(T) triples No={No} Nv={Nv} seed {SEED}"
     ports = [(d, oracle.PreparedPort(oracle.Problem(d)), int(oracle.n_tuples(d["Nv"])))
              for d in systems]
     times, flops = [], 0.0
@@ -239,7 +241,7 @@ def run_reference_arm(args, workload):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload, "systems": desc,
+            "config": {"workload": wl, "name": workload, "systems": desc,
                        "flops_per_step": flops / args.steps, "l2": "inputs > L2"},
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} steps of ~{args.ref_flops:.0e} FLOPs, "
