@@ -249,7 +249,8 @@ __device__ __forceinline__ int energy_rank(int warp, int lane) {
 
 // W cells live in global memory (L2-resident, two buffers per CTA): one
 // 8-byte cell per element, {int32 level-0 sum, float rest} while the groups
-// accumulate, then the FP64 value written over the same 8 bytes.  The
+// accumulate (group 0 writes every cell first, groups 1 and 2 add), then the
+// FP64 value written over the same 8 bytes.  The
 // epilogue warps fill buffer k % 2 for tuple k while the energy warps read
 // buffer (k-1) % 2, so the tensor-core work of one tuple overlaps the FP64
 // energy evaluation of the previous one.
@@ -548,21 +549,32 @@ __global__ void __launch_bounds__(kThreads, 1)
               row[16 + x] = v1[x];
             }
             named_bar_sync(1, 128);
-            const int n = c0 + cc;
             int idx[kMaxRowsPerThread];
             int lev0[kMaxRowsPerThread];
             float rest[kMaxRowsPerThread];
             int2 cell[kMaxRowsPerThread];
 #pragma unroll
             for (int u = 0; u < kMaxRowsPerThread; ++u) {
-              const int r = rq + 4 * u;
+              // cells (r, column): groups 0 and 1 walk the columns across a
+              // warp (W index consecutive in p), group 2 walks r (its W
+              // index is consecutive in r), so every warp access coalesces
+              int r, ccu;
+              if (grp == 2) {
+                const int id = t128 + 128 * u;
+                r = id % No;
+                ccu = id / No;
+              } else {
+                r = rq + 4 * u;
+                ccu = cc;
+              }
+              const int n = c0 + ccu;
               idx[u] = -1;
-              if (r < No && n < nvalid) {
-                lev0[u] = __float2int_rn(stg[r * kStagePitch + cc]);
+              if (r < No && ccu < kStageCols && n < nvalid) {
+                lev0[u] = __float2int_rn(stg[r * kStagePitch + ccu]);
                 float rr = 0.f;
 #pragma unroll
                 for (int q = S - 1; q >= 1; --q)
-                  rr = rr * (1.f / 256.f) + stg[(q * No + r) * kStagePitch + cc];
+                  rr = rr * (1.f / 256.f) + stg[(q * No + r) * kStagePitch + ccu];
                 rest[u] = rr * (1.f / 256.f);
                 const int f = n % No, sl = q0 + n / No;
                 int i, jj, kx;
@@ -572,16 +584,23 @@ __global__ void __launch_bounds__(kThreads, 1)
                 idx[u] = i + No * (jj + No * kx);
               }
             }
+            if (grp == 0) {
+              // group 0 comes first for every cell: plain stores
 #pragma unroll
-            for (int u = 0; u < kMaxRowsPerThread; ++u)
-              if (idx[u] >= 0) cell[u] = __ldcg(&Wc[idx[u]]);
+              for (int u = 0; u < kMaxRowsPerThread; ++u)
+                if (idx[u] >= 0) __stcg(&Wc[idx[u]], make_int2(lev0[u], __float_as_int(rest[u])));
+            } else {
 #pragma unroll
-            for (int u = 0; u < kMaxRowsPerThread; ++u)
-              if (idx[u] >= 0) {
-                cell[u].x += lev0[u];
-                cell[u].y = __float_as_int(__int_as_float(cell[u].y) + rest[u]);
-                __stcg(&Wc[idx[u]], cell[u]);
-              }
+              for (int u = 0; u < kMaxRowsPerThread; ++u)
+                if (idx[u] >= 0) cell[u] = __ldcg(&Wc[idx[u]]);
+#pragma unroll
+              for (int u = 0; u < kMaxRowsPerThread; ++u)
+                if (idx[u] >= 0) {
+                  cell[u].x += lev0[u];
+                  cell[u].y = __float_as_int(__int_as_float(cell[u].y) + rest[u]);
+                  __stcg(&Wc[idx[u]], cell[u]);
+                }
+            }
             named_bar_sync(1, 128);  // the staging buffer is reused
           }
         } else {
@@ -592,19 +611,19 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + buf * K::kBufCols;
           for (int c0 = 0; c0 < NP && okw; c0 += 16) {
             float v[K::kNacc][16];
-  #pragma unroll
+#pragma unroll
             for (int q = 0; q < K::kNacc; ++q) tmem_ld16(tbase + q * NP + c0, v[q]);
             tmem_wait_ld();
             if (valid) {
               // level-0 integer and weighted rest of the 16 columns
               int lev0[16];
               float rest[16];
-  #pragma unroll
+#pragma unroll
               for (int cc = 0; cc < 16; ++cc) {
                 lev0[cc] = __float2int_rn(v[0][cc]);
                 if (SPLIT0) lev0[cc] += __float2int_rn(v[S][cc]);
                 float r = 0.f;
-  #pragma unroll
+#pragma unroll
                 for (int q = S - 1; q >= 1; --q) r = r * (1.f / 256.f) + v[q][cc];
                 rest[cc] = r * (1.f / 256.f);
               }
@@ -612,7 +631,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               // before any store so the round trips to L2 overlap
               int idx[16];
               int2 cell[16];
-  #pragma unroll
+#pragma unroll
               for (int cc = 0; cc < 16; ++cc) {
                 const int col = c0 + cc;
                 int i, jj, kx;
@@ -621,16 +640,24 @@ __global__ void __launch_bounds__(kThreads, 1)
                 else { jj = f; kx = sl; i = col; }
                 idx[cc] = col < No ? i + No * (jj + No * kx) : -1;
               }
-  #pragma unroll
-              for (int cc = 0; cc < 16; ++cc)
-                if (idx[cc] >= 0) cell[cc] = __ldcg(&Wc[idx[cc]]);
-  #pragma unroll
-              for (int cc = 0; cc < 16; ++cc)
-                if (idx[cc] >= 0) {
-                  cell[cc].x += lev0[cc];
-                  cell[cc].y = __float_as_int(__int_as_float(cell[cc].y) + rest[cc]);
-                  __stcg(&Wc[idx[cc]], cell[cc]);
-                }
+              if (grp == 0) {
+                // group 0 comes first for every cell: plain stores
+#pragma unroll
+                for (int cc = 0; cc < 16; ++cc)
+                  if (idx[cc] >= 0)
+                    __stcg(&Wc[idx[cc]], make_int2(lev0[cc], __float_as_int(rest[cc])));
+              } else {
+#pragma unroll
+                for (int cc = 0; cc < 16; ++cc)
+                  if (idx[cc] >= 0) cell[cc] = __ldcg(&Wc[idx[cc]]);
+#pragma unroll
+                for (int cc = 0; cc < 16; ++cc)
+                  if (idx[cc] >= 0) {
+                    cell[cc].x += lev0[cc];
+                    cell[cc].y = __float_as_int(__int_as_float(cell[cc].y) + rest[cc]);
+                    __stcg(&Wc[idx[cc]], cell[cc]);
+                  }
+              }
             }
           }
         }
@@ -685,7 +712,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int i = er; i < No3; i += kEnergyThreads) {
         const int2 cell = Wc[i];
         Wd[i] = unit * ((double)cell.x + (double)__int_as_float(cell.y));
-        if (WSMEM) Wc[i] = make_int2(0, 0);
       }
       __threadfence_block();
       named_bar_sync(2, kEnergyThreads);
@@ -750,18 +776,13 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int2 cell = WJc[i + No * (j + No * kx)];
           return uj * ((double)cell.x + (double)__int_as_float(cell.y));
         });
-        for (int i = er; i < No3; i += kEnergyThreads) WJc[i] = make_int2(0, 0);
-        __threadfence_block();
       }
       if (er == 0) {
         g.e[s.t] = e;
         g.ect[s.t] = ect;
       }
-      if (!WSMEM) {
-        // zero the buffer for the tuple after next, then release it
-        for (int i = er; i < No3; i += kEnergyThreads) Wd[i] = 0.0;
-        __threadfence_block();
-      }
+      // no zeroing: group 0 of the next tuple that uses this buffer writes
+      // every cell without reading it
       named_bar_sync(2, kEnergyThreads);  // Wsm is reused by the next tuple
       if ((!WSMEM || g.use_j) && er == 0) mbar_arrive(&wfree[wb]);
     }
