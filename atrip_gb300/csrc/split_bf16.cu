@@ -247,10 +247,10 @@ __device__ __forceinline__ int energy_rank(int warp, int lane) {
   return ((warp < 4 ? warp - 2 : warp - 6) << 5) | lane;
 }
 
-// W cells live in global memory (L2-resident, two buffers per CTA): one
-// 8-byte cell per element, {int32 level-0 sum, float rest} while the groups
-// accumulate (group 0 writes every cell first, groups 1 and 2 add), then the
-// FP64 value written over the same 8 bytes.  The
+// W cells live in global memory (two tuple parities x passes x three group
+// buffers per CTA): one 8-byte cell per element and group, {int32 level-0
+// sum, float rest}, stored by the epilogue without reading; the energy warps
+// add the three groups into the FP64 value.  The
 // epilogue warps fill buffer k % 2 for tuple k while the energy warps read
 // buffer (k-1) % 2, so the tensor-core work of one tuple overlaps the FP64
 // energy evaluation of the previous one.
@@ -267,7 +267,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char *tail = ring + kStages * K::kStageBytes;
   // W buffers: [tuple parity][pass] per CTA, pass 1 = J intermediates
   const int npass = g.use_j ? 2 : 1;
-  double *Wbase = reinterpret_cast<double *>(g.wglobal) + (size_t)blockIdx.x * 2 * npass * No3;
+  // W buffers: [tuple parity][pass][group] per CTA; each group's items
+  // store their contribution to every cell (no read-modify-write), the
+  // energy warps add the three groups
+  double *Wbase = reinterpret_cast<double *>(g.wglobal) + (size_t)blockIdx.x * 2 * npass * 3 * No3;
   uint64_t *full = reinterpret_cast<uint64_t *>(tail);
   uint64_t *empty = full + kMaxStages;
   uint64_t *accf = empty + kMaxStages;
@@ -517,7 +520,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       ok = wuse == 0 || mbar_wait(&wfree[wb], (wuse - 1) & 1, g.status, kErrTimeoutEmpty);
       for (int it = 0; it < 3 * npass * ntiles; ++it) {
         const int gi = it / ntiles, mt = it % ntiles, grp = gi % 3, pass = gi / 3;
-        int2 *Wc = reinterpret_cast<int2 *>(Wbase + (size_t)(wb * npass + pass) * No3);
+        int2 *Wc = reinterpret_cast<int2 *>(Wbase + (size_t)((wb * npass + pass) * 3 + grp) * No3);
         const int buf = item_count % K::kNbuf;
         const uint32_t use = item_count / K::kNbuf;
         bool okw = ok && alive && mbar_wait(&accf[buf], use & 1, g.status, kErrTimeoutAccFull);
@@ -552,7 +555,6 @@ __global__ void __launch_bounds__(kThreads, 1)
             int idx[kMaxRowsPerThread];
             int lev0[kMaxRowsPerThread];
             float rest[kMaxRowsPerThread];
-            int2 cell[kMaxRowsPerThread];
 #pragma unroll
             for (int u = 0; u < kMaxRowsPerThread; ++u) {
               // cells (r, column): groups 0 and 1 walk the columns across a
@@ -584,23 +586,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                 idx[u] = i + No * (jj + No * kx);
               }
             }
-            if (grp == 0) {
-              // group 0 comes first for every cell: plain stores
 #pragma unroll
-              for (int u = 0; u < kMaxRowsPerThread; ++u)
-                if (idx[u] >= 0) __stcg(&Wc[idx[u]], make_int2(lev0[u], __float_as_int(rest[u])));
-            } else {
-#pragma unroll
-              for (int u = 0; u < kMaxRowsPerThread; ++u)
-                if (idx[u] >= 0) cell[u] = __ldcg(&Wc[idx[u]]);
-#pragma unroll
-              for (int u = 0; u < kMaxRowsPerThread; ++u)
-                if (idx[u] >= 0) {
-                  cell[u].x += lev0[u];
-                  cell[u].y = __float_as_int(__int_as_float(cell[u].y) + rest[u]);
-                  __stcg(&Wc[idx[u]], cell[u]);
-                }
-            }
+            for (int u = 0; u < kMaxRowsPerThread; ++u)
+              if (idx[u] >= 0) __stcg(&Wc[idx[u]], make_int2(lev0[u], __float_as_int(rest[u])));
             named_bar_sync(1, 128);  // the staging buffer is reused
           }
         } else {
@@ -630,7 +618,6 @@ __global__ void __launch_bounds__(kThreads, 1)
               // the 16 cells are distinct elements of W: issue every load
               // before any store so the round trips to L2 overlap
               int idx[16];
-              int2 cell[16];
 #pragma unroll
               for (int cc = 0; cc < 16; ++cc) {
                 const int col = c0 + cc;
@@ -640,24 +627,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 else { jj = f; kx = sl; i = col; }
                 idx[cc] = col < No ? i + No * (jj + No * kx) : -1;
               }
-              if (grp == 0) {
-                // group 0 comes first for every cell: plain stores
 #pragma unroll
-                for (int cc = 0; cc < 16; ++cc)
-                  if (idx[cc] >= 0)
-                    __stcg(&Wc[idx[cc]], make_int2(lev0[cc], __float_as_int(rest[cc])));
-              } else {
-#pragma unroll
-                for (int cc = 0; cc < 16; ++cc)
-                  if (idx[cc] >= 0) cell[cc] = __ldcg(&Wc[idx[cc]]);
-#pragma unroll
-                for (int cc = 0; cc < 16; ++cc)
-                  if (idx[cc] >= 0) {
-                    cell[cc].x += lev0[cc];
-                    cell[cc].y = __float_as_int(__int_as_float(cell[cc].y) + rest[cc]);
-                    __stcg(&Wc[idx[cc]], cell[cc]);
-                  }
-              }
+              for (int cc = 0; cc < 16; ++cc)
+                if (idx[cc] >= 0)
+                  __stcg(&Wc[idx[cc]], make_int2(lev0[cc], __float_as_int(rest[cc])));
             }
           }
         }
@@ -702,16 +675,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (er < No) esm[er] = g.epsi[er];
       const int wb = k & 1;
       ok = mbar_wait(&wfull[wb], (k >> 1) & 1, g.status, kErrTimeoutAccFull);
-      double *Wg = Wbase + (size_t)(wb * npass) * No3;
-      int2 *Wc = reinterpret_cast<int2 *>(Wg);
-      // W = unit * (level-0 integer + rest) in FP64: copied into shared
-      // memory (the buffer is zeroed and handed back to the epilogue at
-      // once), or, when it does not fit, converted in place
+      double *Wg = Wbase + (size_t)(wb * npass) * 3 * No3;
+      const int2 *Wc0 = reinterpret_cast<const int2 *>(Wg);
+      const int2 *Wc1 = Wc0 + No3, *Wc2 = Wc1 + No3;
+      // W = unit * (level-0 integer + rest) in FP64 from the three group
+      // cells (integer parts exact, rests added in group order): copied into
+      // shared memory (the buffers go back to the epilogue at once), or,
+      // when it does not fit, written in place over group 0's cells
       const double unit = g.unit;
       double *Wd = WSMEM ? Wsm : Wg;
       for (int i = er; i < No3; i += kEnergyThreads) {
-        const int2 cell = Wc[i];
-        Wd[i] = unit * ((double)cell.x + (double)__int_as_float(cell.y));
+        const int2 c0 = Wc0[i], c1 = Wc1[i], c2 = Wc2[i];
+        const float rest = (__int_as_float(c0.y) + __int_as_float(c1.y)) + __int_as_float(c2.y);
+        Wd[i] = unit * ((double)(c0.x + c1.x + c2.x) + (double)rest);
       }
       __threadfence_block();
       named_bar_sync(2, kEnergyThreads);
@@ -770,19 +746,22 @@ __global__ void __launch_bounds__(kThreads, 1)
       double ect = e;
       if (g.use_j) {
         // (cT): T from the J pass, Z as above (src/atrip/Atrip.cxx:928-963)
-        int2 *WJc = reinterpret_cast<int2 *>(Wbase + (size_t)(wb * npass + 1) * No3);
+        const int2 *WJ0 = reinterpret_cast<const int2 *>(Wbase + (size_t)(wb * npass + 1) * 3 * No3);
+        const int2 *WJ1 = WJ0 + No3, *WJ2 = WJ1 + No3;
         const double uj = g.unit_j;
         ect = tuple_energy([&](int i, int j, int kx) {
-          const int2 cell = WJc[i + No * (j + No * kx)];
-          return uj * ((double)cell.x + (double)__int_as_float(cell.y));
+          const int x = i + No * (j + No * kx);
+          const int2 c0 = WJ0[x], c1 = WJ1[x], c2 = WJ2[x];
+          const float rest = (__int_as_float(c0.y) + __int_as_float(c1.y)) + __int_as_float(c2.y);
+          return uj * ((double)(c0.x + c1.x + c2.x) + (double)rest);
         });
       }
       if (er == 0) {
         g.e[s.t] = e;
         g.ect[s.t] = ect;
       }
-      // no zeroing: group 0 of the next tuple that uses this buffer writes
-      // every cell without reading it
+      // no zeroing: every group of the next tuple that uses these buffers
+      // stores all of its cells
       named_bar_sync(2, kEnergyThreads);  // Wsm is reused by the next tuple
       if ((!WSMEM || g.use_j) && er == 0) mbar_arrive(&wfree[wb]);
     }
@@ -1214,7 +1193,7 @@ int split_prepare(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
     if (rc != ATRIP_OK) return rc;
   }
   // W buffers (one double per element): two tuple parities x passes per CTA
-  const size_t need = (size_t)sm_count * 2 * (use_j ? 2 : 1) * 2 * No * No * No;  // floats
+  const size_t need = (size_t)sm_count * 2 * (use_j ? 2 : 1) * 3 * 2 * No * No * No;  // floats
   if (need > p->wglobal_floats) {
     s.generation++;
     cudaFree(p->wglobal);
@@ -1235,7 +1214,7 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
     set_error("split form: operands not prepared");
     return ATRIP_ERR_STATE;
   }
-  const size_t need = (size_t)sm_count * 2 * (use_j ? 2 : 1) * 2 * No * No * No;
+  const size_t need = (size_t)sm_count * 2 * (use_j ? 2 : 1) * 3 * 2 * No * No * No;
   if (need > p->wglobal_floats) {
     set_error("split form: W buffers prepared for fewer CTAs");
     return ATRIP_ERR_STATE;
