@@ -227,10 +227,9 @@ struct KernelShapeT {
   static constexpr int kBTile = 256 * 128;
   static constexpr int kStageBytes = kATileBytes + kBTile;
 };
-constexpr int kStageCols = 32;   // epilogue staging: 128 rows x 32 FP32 columns,
-constexpr int kStagePitch = 33;  // padded against bank conflicts
+constexpr int kStageCols = 64;   // epilogue staging: 128 rows x 64 FP32 columns,
+constexpr int kStagePitch = 65;  // padded against bank conflicts
 constexpr int kStagingBytes = 128 * kStagePitch * 4;
-constexpr int kMaxRowsPerThread = 16;  // ceil(No / 4) for No <= 64
 
 // Tuple hand-off ring: the producer owns the work queue and publishes each
 // tuple to the MMA issuer, the epilogue warps and the energy warps.
@@ -531,64 +530,58 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc_fence_after();
         if constexpr (TV) {
           // accumulator: lane s No + r = level s of column r, TMEM column n
-          // = (p,q) pair p + No (q - q0); the four warps stage 32 columns at
+          // = (p,q) pair p + No (q - q0); the four warps stage 64 columns at
           // a time in shared memory, then each thread recombines the levels
-          // of its (r, column) cells and adds them into W
+          // of its (r, column) cells and stores them into the group's W
           const bool okall = named_bar_and(3, 128, okw);
           if (!okall) alive = false;
           const int q0 = mt * jt;
           const int nvalid = No * min(jt, No - q0);
-          const int t128 = threadIdx.x - 128, cc = t128 & 31, rq = t128 >> 5;
+          const int t128 = threadIdx.x - 128, cc = t128 & (kStageCols - 1);
+          const int rq = t128 / kStageCols;  // 0 or 1
+          // floor(x / No) = (x * mno) >> 20 exactly for x < 2^12, No <= 64
+          const uint32_t mno = ((1u << 20) + (uint32_t)No - 1) / (uint32_t)No;
           const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + buf * K::kBufCols;
           for (int c0 = 0; c0 < nvalid && okall; c0 += kStageCols) {
-            float v0[16], v1[16];
-            tmem_ld16(tbase + c0, v0);
-            tmem_ld16(tbase + c0 + 16, v1);
-            tmem_wait_ld();
             float *row = stg + l * kStagePitch;
 #pragma unroll
-            for (int x = 0; x < 16; ++x) {
-              row[x] = v0[x];
-              row[16 + x] = v1[x];
+            for (int h = 0; h < kStageCols / 16; ++h) {
+              float v[16];
+              tmem_ld16(tbase + c0 + 16 * h, v);
+              tmem_wait_ld();
+#pragma unroll
+              for (int x = 0; x < 16; ++x) row[16 * h + x] = v[x];
             }
             named_bar_sync(1, 128);
-            int idx[kMaxRowsPerThread];
-            int lev0[kMaxRowsPerThread];
-            float rest[kMaxRowsPerThread];
-#pragma unroll
-            for (int u = 0; u < kMaxRowsPerThread; ++u) {
-              // cells (r, column): groups 0 and 1 walk the columns across a
-              // warp (W index consecutive in p), group 2 walks r (its W
-              // index is consecutive in r), so every warp access coalesces
+            // cells (r, column): groups 0 and 1 walk the columns across a
+            // warp (W index consecutive in p), group 2 walks r (its W index
+            // is consecutive in r), so every warp store coalesces
+            const int ncells = No * kStageCols;
+            for (int id = t128; id < ncells; id += 128) {
               int r, ccu;
               if (grp == 2) {
-                const int id = t128 + 128 * u;
-                r = id % No;
-                ccu = id / No;
+                ccu = (int)(((uint32_t)id * mno) >> 20);
+                r = id - ccu * No;
               } else {
-                r = rq + 4 * u;
+                r = rq + 2 * ((id - t128) >> 7);
                 ccu = cc;
               }
               const int n = c0 + ccu;
-              idx[u] = -1;
-              if (r < No && ccu < kStageCols && n < nvalid) {
-                lev0[u] = __float2int_rn(stg[r * kStagePitch + ccu]);
-                float rr = 0.f;
+              if (n >= nvalid) continue;
+              const int lev0 = __float2int_rn(stg[r * kStagePitch + ccu]);
+              float rr = 0.f;
 #pragma unroll
-                for (int q = S - 1; q >= 1; --q)
-                  rr = rr * (1.f / 256.f) + stg[(q * No + r) * kStagePitch + ccu];
-                rest[u] = rr * (1.f / 256.f);
-                const int f = n % No, sl = q0 + n / No;
-                int i, jj, kx;
-                if (grp == 0) { i = f; jj = sl; kx = r; }
-                else if (grp == 1) { i = f; kx = sl; jj = r; }
-                else { jj = f; kx = sl; i = r; }
-                idx[u] = i + No * (jj + No * kx);
-              }
+              for (int q = S - 1; q >= 1; --q)
+                rr = rr * (1.f / 256.f) + stg[(q * No + r) * kStagePitch + ccu];
+              const int nq = (int)(((uint32_t)n * mno) >> 20);
+              const int f = n - nq * No, sl = q0 + nq;
+              int i, jj, kx;
+              if (grp == 0) { i = f; jj = sl; kx = r; }
+              else if (grp == 1) { i = f; kx = sl; jj = r; }
+              else { jj = f; kx = sl; i = r; }
+              __stcg(&Wc[i + No * (jj + No * kx)],
+                     make_int2(lev0, __float_as_int(rr * (1.f / 256.f))));
             }
-#pragma unroll
-            for (int u = 0; u < kMaxRowsPerThread; ++u)
-              if (idx[u] >= 0) __stcg(&Wc[idx[u]], make_int2(lev0[u], __float_as_int(rest[u])));
             named_bar_sync(1, 128);  // the staging buffer is reused
           }
         } else {
@@ -1131,8 +1124,12 @@ int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t 
   return ATRIP_OK;
 }
 
+// S slices of No rows fit the 128 M rows, level 0 stays exact (K <= 1024),
+// and two 48 KB operand stages fit next to the singles blocks and staging.
 bool transposed_eligible(int S, int No, int Nv) {
-  return S * No <= 128 && 2 * (Nv + No) <= 1024;
+  const size_t fixed = 1024 + kTailBytes + kStagingBytes + sizeof(double) * 3 * No * No;
+  return S * No <= 128 && 2 * (Nv + No) <= 1024 &&
+         fixed + 2 * (size_t)KernelShapeT<2>::kStageBytes <= (size_t)kSmemLimit;
 }
 
 template <int S>
