@@ -192,7 +192,7 @@ def tune_split(ctx: capi.Context, slices: int, flops: float = 2e13, m: int = 8) 
         best_ms, tuning = t, c
     # then the processing order: tuples grouped by (a, b, c) blocks of side L
     # keep the slabs of the tuples in flight in L2
-    for L in (4, 6, 8, 12):
+    for L in (4, 6, 8, 12, 16, 24):
         c = dict(tuning, tuple_block=L)
         t = _time(ctx, wins, "split_bf16", slices, c)
         timed.append((t, c))

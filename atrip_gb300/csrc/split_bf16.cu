@@ -27,14 +27,17 @@
 // get_energy_{distinct,same} (src/atrip/Equations.cxx:101-238, 387-426) in
 // FP64.
 //
-// Kernel roles (256 threads, one persistent CTA per SM):
-//   warp 0      TMA producer: A slice tile + the B slice tiles it pairs with
-//   warp 1      TMEM owner and single-thread tcgen05.mma issuer
-//   warps 4..7  epilogue: tcgen05.ld of the level accumulators, scatter-add
-//               into W at the group's index permutation
-//   all warps   energy loop and reduction at the end of each tuple
+// Kernel roles (512 threads, one persistent CTA per SM):
+//   warp 0          TMA producer: owns the tuple queue, loads the operand
+//                   tiles of every unit into the shared-memory ring
+//   warp 1          TMEM owner and single-thread tcgen05.mma issuer
+//   warps 4..7      epilogue: tcgen05.ld of the accumulators, level
+//                   recombination, stores of the group's W cells
+//   warps 2, 3, 8..15  energy: W in FP64, Zijk, get_energy_{distinct,same}
+//                   and the block reduction, one tuple behind the MMAs
 // Smem ring of operand stages (full/empty mbarriers), two TMEM accumulator
-// buffers (full/empty mbarriers); every wait is bounded (sm100.cuh).
+// buffers (full/empty mbarriers), a 4-slot tuple hand-off ring and two W
+// buffer sets; every wait is bounded (sm100.cuh).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -54,7 +57,7 @@ namespace {
 
 using namespace sm100;
 
-constexpr int kThreads = 448;
+constexpr int kThreads = 512;
 constexpr int kMaxStages = 6;
 constexpr int kSmemLimit = 232448;  // opt-in dynamic shared memory per block
 constexpr int kTailBytes = 384 + 3 * 64 * 8 + 16 * 8 + 64 * 8;  // + singles blocks (+ W copy)
@@ -234,7 +237,7 @@ constexpr int kStagingBytes = 128 * kStagePitch * 4;
 // Tuple hand-off ring: the producer owns the work queue and publishes each
 // tuple to the MMA issuer, the epilogue warps and the energy warps.
 constexpr int kTupleSlots = 4;
-constexpr int kEnergyWarps = 8;  // warps 2, 3 and 8 .. 13
+constexpr int kEnergyWarps = 10;  // warps 2, 3 and 8 .. 15
 constexpr int kEnergyThreads = kEnergyWarps * 32;
 
 struct TupleSlot {
@@ -638,8 +641,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (threadIdx.x == 128) mbar_arrive(&wfull[wb]);
     }
     __syncwarp();
-  } else if (warp < 14) {
-    // ------------------------------------------------ energy (8 warps)
+  } else if (warp < 16) {
+    // ------------------------------------------------ energy (10 warps)
     const int er = energy_rank(warp, lane);
     const int64_t Nv = g.Nv;
     for (uint32_t k = 0;; ++k) {
