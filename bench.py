@@ -476,6 +476,21 @@ def run_batch96(args, world, rank, local):
     tiles = autotune.tune_batch_tiles(ctxs)
     b = capi.Batch(ctxs)
     btune = autotune.tune_batch(b)
+    split_choice = None
+    if form != "fp64":
+        # split kernel variant and processing order for the batch: one full
+        # batch run per candidate, the faster kept
+        base = [c.get_tuning() for c in ctxs]
+        trials = []
+        for cand in ({}, {"split_variant": 2}, {"split_variant": 2, "tuple_block": 4}):
+            for c, t in zip(ctxs, base):
+                c.set_tuning(**dict(t, **cand))
+            b.run(form=form, slices=slices, use_j=False)  # first run captures the graph
+            ms = b.run(form=form, slices=slices, use_j=False)[0].device_ms
+            trials.append((ms, cand))
+        split_choice = min(trials, key=lambda x: x[0])
+        for c, t in zip(ctxs, base):
+            c.set_tuning(**dict(t, **split_choice[1]))
     stream = torch.cuda.Stream()
 
     def step(s):
@@ -543,7 +558,9 @@ def run_batch96(args, world, rank, local):
                                "seeds 0..95", "name": "batch96", "form": form, "slices": slices,
                    "tuples_per_step": total_tuples, "flops_per_step": total_flops,
                    "fp64_row_tiles": {"32": tiles.count(32), "64": tiles.count(64)},
-                   "batch_tuning": btune["tuning"], "l2": "no flush: inputs > 129 MB L2",
+                   "batch_tuning": btune["tuning"],
+                   "split_tuning": split_choice[1] if split_choice else None,
+                   "l2": "no flush: inputs > 129 MB L2",
                    "time_to_ET_s": ms / args.steps / 1e3, "input_gen_s": t_gen},
         "compare_fp64": compare,
         "roofline": roof,
