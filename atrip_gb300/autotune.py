@@ -182,6 +182,8 @@ def tune_split(ctx: capi.Context, slices: int, flops: float = 2e13, m: int = 8) 
         # transposed kernel: stacked slices as M, (p,q) pairs as N <= 256
         cands += [{"split_variant": 2, "split_stages": st} for st in (0, 3)]
         cands += [{"split_variant": 2, "split_w_global": 1}]
+        if ctx.No % 8 == 0:  # one shared stack load per K chunk
+            cands += [{"split_variant": 3}]
     timed = [(_time(ctx, wins, "split_bf16", slices, c), c) for c in cands]
     best_ms, tuning = min(timed, key=lambda x: x[0])
     # L2 prefetch of the next part's slab tiles

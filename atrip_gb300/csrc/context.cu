@@ -530,8 +530,8 @@ int atrip_gpu_set_tuning(atrip_gpu_context *c, const atrip_tuning *t) {
     return fail(ATRIP_ERR_ARGUMENT, "negative tuning value");
   if (t->fp64_tile_rows != 0 && t->fp64_tile_rows != 32 && t->fp64_tile_rows != 64)
     return fail(ATRIP_ERR_ARGUMENT, "fp64_tile_rows must be 32 or 64");
-  if (t->split_variant < 0 || t->split_variant > 2)
-    return fail(ATRIP_ERR_ARGUMENT, "split_variant must be 0, 1 or 2");
+  if (t->split_variant < 0 || t->split_variant > 3)
+    return fail(ATRIP_ERR_ARGUMENT, "split_variant must be 0..3");
   if (t->tuple_block < 0 || t->tuple_block > 1023)
     return fail(ATRIP_ERR_ARGUMENT, "tuple_block must be in [0, 1023]");
   if (t->split_stages != 0 && (t->split_stages < 2 || t->split_stages > 6))

@@ -78,12 +78,16 @@ struct SplitMaps {
   // transposed variant: boxes of jt2 (p,q) row groups for the N side, all S
   // slices stacked for the M side
   CUtensorMap TaN2, TaT2, VhN2, VhT2, Vp2, TpN2, TpT2, JhN2, JhT2, Jp2;
+  // ... and the r-column operand with 2S-1 slices, one load per K chunk
+  // shared by the S slice units (MSHARE)
+  CUtensorMap Vp3, TpN3, TpT3, Jp3;
 };
 
 struct SplitArgs {
   int No, Nv, jt, ntiles, kch;  // j per M-tile, M-tiles per group, K chunks of Nv
   int jt2, ntiles2, nmma;       // transposed variant: q per N-tile, N-tiles, MMA N
   int prefetch;                 // 1: L2 prefetch of the next part's (p,q)-row tiles
+  int mslot_bytes;              // MSHARE: bytes of one shared M-tile slot
   int nstages;                 // operand ring depth
   const double *epsi, *epsa, *tai, *Vhh;
   const uint32_t *tuples, *triples;
@@ -161,7 +165,7 @@ __device__ __forceinline__ bool named_bar_and(int id, int n, bool v) {
 }
 
 struct Part {
-  const CUtensorMap *amap, *bmap;
+  const CUtensorMap *amap, *bmap, *bmap3;
   int ax, bz, by;  // A: tensor index (x or w); B: (z, y) or (v, u)
   bool particle;
 };
@@ -191,6 +195,7 @@ __device__ __forceinline__ Part part_of(const SplitMaps &m, int g, int pt, int a
     p.amap = tv ? (tr ? &m.TaT2 : &m.TaN2) : (tr ? &m.TaT : &m.TaN);
     p.ax = x;
     p.bmap = tv ? (pass ? &m.Jp2 : &m.Vp2) : (pass ? &m.Jp : &m.Vp);
+    p.bmap3 = pass ? &m.Jp3 : &m.Vp3;
     p.bz = z;
     p.by = y;
   } else {
@@ -198,6 +203,7 @@ __device__ __forceinline__ Part part_of(const SplitMaps &m, int g, int pt, int a
                 : (pass ? (tr ? &m.JhT : &m.JhN) : (tr ? &m.VhT : &m.VhN));
     p.ax = w;
     p.bmap = tv ? (holeT ? &m.TpT2 : &m.TpN2) : (holeT ? &m.TpT : &m.TpN);
+    p.bmap3 = holeT ? &m.TpT3 : &m.TpN3;
     p.bz = v;
     p.by = u;
   }
@@ -220,7 +226,7 @@ struct KernelShape {
 // operand stacked (row s No + r), N = nmma <= 256 columns of (p,q) pairs,
 // one 128 x 256 FP32 accumulator per item, double-buffered (all 512 TMEM
 // columns).  Stage: 16 KB M-side tile + 32 KB N-side tile.
-template <int S>
+template <int S, bool MSHARE = false>
 struct KernelShapeT {
   static constexpr int kNacc = 1;
   static constexpr int kBufCols = 256;
@@ -228,8 +234,11 @@ struct KernelShapeT {
   static constexpr int kCols = 512;
   static constexpr int kAllocCols = 512;
   static constexpr int kBTile = 256 * 128;
-  static constexpr int kStageBytes = kATileBytes + kBTile;
+  // MSHARE: the ring holds N-side tiles only; the M-side stacks live in two
+  // separate slots, one per K chunk, shared by its S slice units
+  static constexpr int kStageBytes = (MSHARE ? 0 : kATileBytes) + kBTile;
 };
+constexpr int kMSlots = 2;
 constexpr int kStageCols = 64;   // epilogue staging: 128 rows x 64 FP32 columns,
 constexpr int kStagePitch = 65;  // padded against bank conflicts
 constexpr int kStagingBytes = 128 * kStagePitch * 4;
@@ -256,17 +265,18 @@ __device__ __forceinline__ int energy_rank(int warp, int lane) {
 // epilogue warps fill buffer k % 2 for tuple k while the energy warps read
 // buffer (k-1) % 2, so the tensor-core work of one tuple overlaps the FP64
 // energy evaluation of the previous one.
-template <int S, int NP, bool SPLIT0, bool WSMEM, bool TV>
+template <int S, int NP, bool SPLIT0, bool WSMEM, bool TV, bool MSHARE = false>
 __global__ void __launch_bounds__(kThreads, 1)
     triples_split_kernel(const __grid_constant__ SplitMaps maps, const SplitArgs g) {
-  using K = typename std::conditional<TV, KernelShapeT<S>, KernelShape<S, NP, SPLIT0>>::type;
+  using K = typename std::conditional<TV, KernelShapeT<S, MSHARE>, KernelShape<S, NP, SPLIT0>>::type;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char *ring = smem;
   const int No = g.No, No2 = No * No, No3 = No2 * No;
   const int kStages = g.nstages;
-  unsigned char *tail = ring + kStages * K::kStageBytes;
+  unsigned char *mring = ring + kStages * K::kStageBytes;  // MSHARE slots
+  unsigned char *tail = mring + (MSHARE ? kMSlots * g.mslot_bytes : 0);
   // W buffers: [tuple parity][pass] per CTA, pass 1 = J intermediates
   const int npass = g.use_j ? 2 : 1;
   // W buffers: [tuple parity][pass][group] per CTA; each group's items
@@ -281,8 +291,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t *tempty = tfull + kTupleSlots;
   uint64_t *wfull = tempty + kTupleSlots;
   uint64_t *wfree = wfull + 2;
-  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(wfree + 2);
-  TupleSlot *tslot = reinterpret_cast<TupleSlot *>(tail + 256);
+  uint64_t *mfull = wfree + 2;  // MSHARE slot barriers
+  uint64_t *mempty = mfull + kMSlots;
+  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(mempty + kMSlots);
+  TupleSlot *tslot = reinterpret_cast<TupleSlot *>(tail + 264);
   double *ta = reinterpret_cast<double *>(tail + 384);
   double *tb = ta + 64;
   double *tc = tb + 64;
@@ -303,6 +315,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&acce[b], 128);
       mbar_init(&wfull[b], 1);
       mbar_init(&wfree[b], 1);
+      mbar_init(&mfull[b], 1);
+      mbar_init(&mempty[b], 1);
     }
     for (int s = 0; s < kTupleSlots; ++s) {
       mbar_init(&tfull[s], 1);
@@ -323,7 +337,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   }
   // rows of the A stage tiles past No*jt are never written by TMA: zero them
-  for (int i = threadIdx.x; i < kStages * K::kStageBytes / 16; i += kThreads)
+  for (int i = threadIdx.x;
+       i < (kStages * K::kStageBytes + (MSHARE ? kMSlots * g.mslot_bytes : 0)) / 16;
+       i += kThreads)
     reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
   if (warp == 1) {
     tmem_alloc(tmem_holder, K::kAllocCols);
@@ -339,7 +355,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     // ------------------------------------------------------ TMA producer
     if (lane == 0) {
-      uint32_t unit_count = 0;
+      uint32_t unit_count = 0, mcount = 0;
       bool alive = true;
       for (uint32_t k = 0;; ++k) {
         const int ts = k % kTupleSlots;
@@ -384,6 +400,24 @@ __global__ void __launch_bounds__(kThreads, 1)
               }
               for (int ch = 0; ch < nch && alive; ++ch)
                 for (int sa = 0; sa < S; ++sa) {
+                  if constexpr (MSHARE) {
+                    if (sa == 0) {
+                      // one M-side stack per K chunk: slices -(S-1) .. S-1
+                      // (the negative ones read as zeros); slice unit sa
+                      // uses the 128 rows from row block S-1-sa
+                      const int ms = mcount % kMSlots;
+                      const uint32_t muse = mcount / kMSlots;
+                      if (muse > 0 &&
+                          !mbar_wait(&mempty[ms], (muse - 1) & 1, g.status, kErrTimeoutEmpty)) {
+                        alive = false;
+                        break;
+                      }
+                      mbar_arrive_expect_tx(&mfull[ms], 128 * (2 * S - 1) * No);
+                      tma_load_5d(mring + ms * g.mslot_bytes, p.bmap3, &mfull[ms], ch * kKChunk,
+                                  0, p.bz, p.by, -(S - 1));
+                      ++mcount;
+                    }
+                  }
                   const int st = unit_count % kStages;
                   const uint32_t use = unit_count / kStages;
                   if (use > 0 && !mbar_wait(&empty[st], (use - 1) & 1, g.status, kErrTimeoutEmpty)) {
@@ -391,7 +425,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                   }
                   unsigned char *sbase = ring + st * K::kStageBytes;
-                  if constexpr (TV) {
+                  if constexpr (MSHARE) {
+                    mbar_arrive_expect_tx(&full[st], a_bytes);
+                    tma_load_5d(sbase, p.amap, &full[st], ch * kKChunk, 0, j0, p.ax, sa);
+                  } else if constexpr (TV) {
                     // M side: slices -sa .. S-1-sa of the r-column operand
                     // (those below 0 read as zeros), so row block j always
                     // holds level j = sa + sb; N side: (p,q) rows, slice sa
@@ -417,7 +454,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == 1) {
     // -------------------------------------------------------- MMA issuer
     if (lane == 0) {
-      uint32_t unit_count = 0, item_count = 0;
+      uint32_t unit_count = 0, item_count = 0, mcount = 0;
       bool alive = true;
       for (uint32_t k = 0;; ++k) {
         const int ts = k % kTupleSlots;
@@ -442,7 +479,15 @@ __global__ void __launch_bounds__(kThreads, 1)
               // particle chunk) and past No (hole chunk) is skipped
               const int kvalid = (pt & 1) == 0 ? min(kKChunk, g.Nv - ch * kKChunk) : g.No;
               const int nkk = (kvalid + 15) / 16;
+              const int ms = mcount % kMSlots;
               for (int sa = 0; sa < S; ++sa) {
+                if constexpr (MSHARE) {
+                  if (sa == 0 &&
+                      !mbar_wait(&mfull[ms], (mcount / kMSlots) & 1, g.status, kErrTimeoutFull)) {
+                    alive = false;
+                    break;
+                  }
+                }
                 const int st = unit_count % kStages;
                 const uint32_t use_s = unit_count / kStages;
                 if (!mbar_wait(&full[st], use_s & 1, g.status, kErrTimeoutFull)) {
@@ -451,8 +496,13 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 tc_fence_after();
                 const uint32_t sbase = smem_u32(ring + st * K::kStageBytes);
-                const uint64_t adesc = sdesc_sw128(sbase);
-                const uint64_t bdesc = sdesc_sw128(sbase + kATileBytes);
+                // MSHARE: A = the chunk's shared stack from row block S-1-sa
+                // (No % 8 == 0 keeps the start on a 1024-byte swizzle atom)
+                const uint64_t adesc =
+                    MSHARE ? sdesc_sw128(smem_u32(mring + ms * g.mslot_bytes) +
+                                         (uint32_t)((S - 1 - sa) * No * 128))
+                           : sdesc_sw128(sbase);
+                const uint64_t bdesc = sdesc_sw128(MSHARE ? sbase : sbase + kATileBytes);
                 // A slice sa against B slices 0 .. S-1-sa in one MMA: the
                 // result columns are the level accumulators sa .. S-1, which
                 // sit side by side in TMEM.  (Transposed variant: the stacked
@@ -492,6 +542,12 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 mma_commit(&empty[st]);
                 ++unit_count;
+                if constexpr (MSHARE) {
+                  if (sa == S - 1) {
+                    mma_commit(&mempty[ms]);  // the stack is free once these MMAs end
+                    ++mcount;
+                  }
+                }
               }
             }
           }
@@ -989,12 +1045,25 @@ int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, cudaSt
     if ((rc = make_map(&p->maps.TpN2, p->TpS, d, box))) return rc;
     if ((rc = make_map(&p->maps.TpT2, p->TpTS, d, box))) return rc;
   }
+  // shared M stacks: 2S-1 slices from slice -(S-1)
+  {
+    const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)(2 * S - 1)};
+    if ((rc = make_map(&p->maps.Vp3, p->VpS, d, box))) return rc;
+  }
+  {
+    const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)(2 * S - 1)};
+    if ((rc = make_map(&p->maps.TpN3, p->TpS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.TpT3, p->TpTS, d, box))) return rc;
+  }
   p->maps.JhN = p->maps.VhN;
   p->maps.JhT = p->maps.VhT;
   p->maps.Jp = p->maps.Vp;
   p->maps.JhN2 = p->maps.VhN2;
   p->maps.JhT2 = p->maps.VhT2;
   p->maps.Jp2 = p->maps.Vp2;
+  p->maps.Jp3 = p->maps.Vp3;
   return ATRIP_OK;
 }
 
@@ -1056,6 +1125,11 @@ int prepare_j(SplitImpl *p, const DeviceTensors &dt, cudaStream_t st, int64_t *l
     const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)S};
     if ((rc = make_map(&p->maps.Jp2, p->JpS, d, box))) return rc;
   }
+  {
+    const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
+    const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)(2 * S - 1)};
+    if ((rc = make_map(&p->maps.Jp3, p->JpS, d, box))) return rc;
+  }
   p->has_j = true;
   return ATRIP_OK;
 }
@@ -1100,12 +1174,19 @@ int launch_np(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
 
 // Transposed variant (S No <= 128, K = 2 (Nv + No) <= 1024).  The FP64 copy
 // of W goes to shared memory when at least three operand stages still fit.
-template <int S, bool WSMEM>
+// One shared M slot: (S-1) No + 128 rows of 128 bytes (the MMA of slice
+// unit sa reads 128 rows from row (S-1-sa) No), on 1024-byte atoms.
+size_t mslot_bytes_for(int S, int No) {
+  return ((size_t)((S - 1) * No + 128) * 128 + 1023) / 1024 * 1024;
+}
+
+template <int S, bool WSMEM, bool MSHARE>
 int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
-  using K = KernelShapeT<S>;
+  using K = KernelShapeT<S, MSHARE>;
   const size_t No3 = (size_t)a.No * a.No * a.No;
+  const size_t mslots = MSHARE ? kMSlots * mslot_bytes_for(S, a.No) : 0;
   const size_t vbytes =
-      sizeof(double) * (3 * (size_t)a.No * a.No + (WSMEM ? No3 : 0)) + kStagingBytes;
+      sizeof(double) * (3 * (size_t)a.No * a.No + (WSMEM ? No3 : 0)) + kStagingBytes + mslots;
   const size_t avail = kSmemLimit - 1024 - kTailBytes - vbytes;
   int nst = (int)(avail / K::kStageBytes);
   if (nst > kMaxStages) nst = kMaxStages;
@@ -1116,8 +1197,9 @@ int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t 
   }
   SplitArgs args = a;
   args.nstages = nst;
+  args.mslot_bytes = MSHARE ? (int)mslot_bytes_for(S, a.No) : 0;
   const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
-  auto kern = triples_split_kernel<S, 16, false, WSMEM, true>;
+  auto kern = triples_split_kernel<S, 16, false, WSMEM, true, MSHARE>;
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   const int64_t n = a.t_end - a.t_begin;
@@ -1139,16 +1221,22 @@ template <int S>
 int launch_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   const size_t No3 = (size_t)a.No * a.No * a.No;
   const size_t fixed = 1024 + kTailBytes + kStagingBytes + sizeof(double) * 3 * a.No * a.No;
+  // variant 3: one M stack per K chunk shared by the S slice units, where
+  // its row blocks start on swizzle atoms (No % 8 == 0) and 2 ring stages fit
+  if (p->variant == 3 && a.No % 8 == 0 &&
+      fixed + kMSlots * mslot_bytes_for(S, a.No) + 2 * KernelShapeT<S, true>::kStageBytes <=
+          (size_t)kSmemLimit)
+    return launch_shape_t<S, false, true>(p, a, sm_count, st);
   const bool wsmem =
       !p->w_global && fixed + sizeof(double) * No3 + 3 * KernelShapeT<S>::kStageBytes <=
                           (size_t)kSmemLimit;
-  return wsmem ? launch_shape_t<S, true>(p, a, sm_count, st)
-               : launch_shape_t<S, false>(p, a, sm_count, st);
+  return wsmem ? launch_shape_t<S, true, false>(p, a, sm_count, st)
+               : launch_shape_t<S, false, false>(p, a, sm_count, st);
 }
 
 template <int S>
 int launch_s(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
-  if (p->variant == 2 && transposed_eligible(S, a.No, a.Nv))
+  if (p->variant >= 2 && transposed_eligible(S, a.No, a.Nv))
     return launch_t<S>(p, a, sm_count, st);
   const int No = a.No;
   if (No <= 16) return launch_np<S, 16>(p, a, sm_count, st);

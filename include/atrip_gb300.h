@@ -163,7 +163,9 @@ typedef struct {
   int32_t split_variant;    /* split form kernel: 0/1 = M tiles of (p,q) rows;     */
                             /* 2 = transposed (the S slices of V stacked as the    */
                             /* M rows, up to 256 (p,q) pairs as N) where S No <=   */
-                            /* 128 and 2 (Nv + No) <= 1024, else variant 1          */
+                            /* 128 and 2 (Nv + No) <= 1024, else variant 1;        */
+                            /* 3 = 2 with one stack load per K chunk shared by the */
+                            /* S slice units (No % 8 == 0), else variant 2          */
   int32_t split_prefetch;   /* split form: 1 = prefetch the next part's T / V_hhhp  */
                             /* slab tiles into L2 while the current part streams   */
 } atrip_tuning;

@@ -33,10 +33,12 @@ CASES = [(6, 10, 1), (8, 40, 0), (5, 9, 3), (13, 17, 2), (24, 30, 4), (30, 14, 5
 
 @pytest.mark.parametrize("No,Nv,seed", CASES)
 @pytest.mark.parametrize("S", [2, 3, 4])
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 2, 3])
 def test_split_matches_model_and_fp64(No, Nv, seed, S, variant):
     """variant 2 = the transposed kernel (stacked slices as the MMA's M rows)
-    where S No <= 128; elsewhere it falls back to variant 1."""
+    where S No <= 128, elsewhere variant 1; variant 3 = variant 2 with one
+    stack load per K chunk shared by the slice units where No % 8 == 0,
+    elsewhere variant 2."""
     d = synth.make_inputs(No, Nv, seed)
     n = min(synth.n_tuples(Nv), 120)
     model = split_model.split_tuple_energies(d, S, 0, n)
@@ -169,7 +171,8 @@ def test_transposed_variant_with_j_and_knobs(No, Nv, seed, S):
         for tune in ({"split_variant": 2}, {"split_variant": 2, "split_w_global": 1},
                      {"split_variant": 2, "split_stages": 2, "tuple_block": 4},
                      {"split_variant": 2, "split_prefetch": 1},
-                     {"split_variant": 1, "split_prefetch": 1}):
+                     {"split_variant": 1, "split_prefetch": 1},
+                     {"split_variant": 3}, {"split_variant": 3, "tuple_block": 4}):
             ctx.set_tuning(**tune)
             ctx.run(form="split_bf16", slices=S, use_j=True, max_iterations=n - 1)
             e2, c2 = ctx.tuple_energies(0, n)
