@@ -8,9 +8,11 @@ keeps the fastest:
 * FP64 form: the register tile (32 or 64 rows of (p,q) pairs per CTA pass),
   the kernel's register budget (compiler's choice, or capped at 128 for two
   resident CTAs per SM) and the tuples a CTA claims per queue access;
-* split form: the slice count first -- the smallest S in 2..4 whose
-  estimated |dE(T)| against the FP64 form, carried to the power-of-two scaled
-  twin of the system with |E(T)| ~ 0.1 Eh, stays within ``tol_eh`` -- then
+* split forms: the slice format first -- the cheapest of 2 FP16 slices
+  (where the system fits its kernel; form ``split``) and 2..4 BF16 slices
+  whose estimated |dE(T)| against the FP64 form, carried to the
+  power-of-two scaled twin of the system with |E(T)| ~ 0.1 Eh, stays within
+  ``tol_eh`` -- then
   the depth of the operand ring, where W lives (shared memory or L2) and the
   processing order (list order, or grouped in (a, b, c) blocks of side L so
   the tuples in flight share their operand slabs in L2).
@@ -153,42 +155,69 @@ def tune_fp64(ctx: capi.Context, flops: float = 2e12, m: int = 8) -> dict:
             "sample_tuples": sum(hi - lo for lo, hi in wins)}
 
 
+def f16_eligible(No: int, Nv: int) -> bool:
+    """The FP16 form's kernel: 2 slices of No rows in the 128 M rows with two
+    operand stages beside the singles blocks in shared memory (No <= 63),
+    level-0 sums below 2^31 (K = 2 (Nv + No) < 2048)."""
+    return No <= 63 and 2 * (Nv + No) < 2048
+
+
+def split_formats(No: int, Nv: int, form: str = "split", slice_counts=(2, 3, 4)):
+    """(form, slices) candidates in order of tensor-core work: 2 FP16 slices
+    (3 digit products, 22-bit digits) replace 2 BF16 slices (3 products,
+    16 bits) where the FP16 kernel covers the system."""
+    out = []
+    if form in ("split", "split_f16") and f16_eligible(No, Nv):
+        out.append(("split_f16", 2))
+    if form != "split_f16":
+        out += [("split_bf16", S) for S in slice_counts if not (out and S == 2)]
+    return out
+
+
 def choose_slices(ctx: capi.Context, tol_eh: float = 1e-8, flops: float = 2e12, m: int = 16,
-                  slice_counts=(2, 3, 4)) -> dict:
-    """Smallest slice count whose twin error bound is within tol_eh."""
+                  slice_counts=(2, 3, 4), form: str = "split_bf16") -> dict:
+    """Cheapest slice format whose twin error bound is within tol_eh."""
     n = capi.n_tuples(ctx.Nv)
     wins = windows(n, m, window_size(ctx.No, ctx.Nv, m, flops))
     _, e_ref = run_windows(ctx, wins, "fp64")
     report = {}
-    chosen = max(slice_counts)
-    for S in slice_counts:
-        _, e_s = run_windows(ctx, wins, "split_bf16", S)
+    cands = split_formats(ctx.No, ctx.Nv, form, slice_counts)
+    chosen = cands[-1]
+    for f, S in cands:
+        _, e_s = run_windows(ctx, wins, f, S)
         est = error_estimate(n, e_ref, e_s)
-        report[S] = est
+        report[f"{f}x{S}"] = est
         if est["twin_dE_bound"] <= tol_eh:
-            chosen = S
+            chosen = (f, S)
             break
-    return {"slices": chosen, "estimates": report}
+    return {"form": chosen[0], "slices": chosen[1], "estimates": report}
 
 
-def tune_split(ctx: capi.Context, slices: int, flops: float = 2e13, m: int = 8) -> dict:
+def tune_split(ctx: capi.Context, slices: int, flops: float = 2e13, m: int = 8,
+               form: str = "split_bf16") -> dict:
     n = capi.n_tuples(ctx.Nv)
     wins = windows(n, m, window_size(ctx.No, ctx.Nv, m, flops))
-    run_windows(ctx, wins[:1], "split_bf16", slices)  # warm-up (cuts the slices)
+    run_windows(ctx, wins[:1], form, slices)  # warm-up (cuts the slices)
+    f16 = form == "split_f16"  # always the transposed kernel
     cands = [{"split_stages": st} for st in (0, 3, 4)]
-    if ctx.No <= 24:  # W copy in shared memory, or a deeper ring with W in L2
+    if ctx.No <= 24 and not f16:  # W copy in shared memory, or a deeper ring with W in L2
         cands += [{"split_stages": st, "split_w_global": 1} for st in (0, 5)]
-    if slices * ctx.No <= 128 and 2 * (ctx.Nv + ctx.No) <= 1024:
+    if f16:
+        cands = [{"split_variant": 2, "split_stages": st} for st in (0, 3)]
+        cands += [{"split_variant": 2, "split_w_global": 1}]
+        if ctx.No % 8 == 0:
+            cands += [{"split_variant": 3}]
+    elif slices * ctx.No <= 128 and 2 * (ctx.Nv + ctx.No) <= 1024:
         # transposed kernel: stacked slices as M, (p,q) pairs as N <= 256
         cands += [{"split_variant": 2, "split_stages": st} for st in (0, 3)]
         cands += [{"split_variant": 2, "split_w_global": 1}]
         if ctx.No % 8 == 0:  # one shared stack load per K chunk
             cands += [{"split_variant": 3}]
-    timed = [(_time(ctx, wins, "split_bf16", slices, c), c) for c in cands]
+    timed = [(_time(ctx, wins, form, slices, c), c) for c in cands]
     best_ms, tuning = min(timed, key=lambda x: x[0])
     # L2 prefetch of the next part's slab tiles
     c = dict(tuning, split_prefetch=1)
-    t = _time(ctx, wins, "split_bf16", slices, c)
+    t = _time(ctx, wins, form, slices, c)
     timed.append((t, c))
     if t < 0.98 * best_ms:
         best_ms, tuning = t, c
@@ -196,7 +225,7 @@ def tune_split(ctx: capi.Context, slices: int, flops: float = 2e13, m: int = 8) 
     # keep the slabs of the tuples in flight in L2
     for L in (4, 6, 8, 12, 16, 24):
         c = dict(tuning, tuple_block=L)
-        t = _time(ctx, wins, "split_bf16", slices, c)
+        t = _time(ctx, wins, form, slices, c)
         timed.append((t, c))
         if t < 0.98 * best_ms:
             best_ms, tuning = t, c
@@ -206,8 +235,9 @@ def tune_split(ctx: capi.Context, slices: int, flops: float = 2e13, m: int = 8) 
 
 def tune(ctx: capi.Context, form: str = "split_bf16", tol_eh: float = 1e-8,
          use_cache: bool = True, slices: int = 0) -> dict:
-    """Tune ctx for form; returns {"tuning": ..., "slices": ...} and applies
-    the tuning to ctx.  slices=0 lets the tuner choose."""
+    """Tune ctx for form; returns {"tuning": ..., "form": ..., "slices": ...}
+    and applies the tuning to ctx.  slices=0 lets the tuner choose; form
+    "split" lets it choose between the FP16 and BF16 split forms too."""
     key = _key(ctx, form) + (f"|S={slices}" if slices else "")
     cache = _load_cache() if use_cache else {}
     if key in cache:
@@ -217,11 +247,15 @@ def tune(ctx: capi.Context, form: str = "split_bf16", tol_eh: float = 1e-8,
     t0 = time.perf_counter()
     if form == "fp64":
         r = tune_fp64(ctx)
-        ent = {"tuning": r["tuning"], "slices": 0, "detail": {"fp64": r}}
+        ent = {"tuning": r["tuning"], "form": "fp64", "slices": 0, "detail": {"fp64": r}}
     else:
-        acc = choose_slices(ctx, tol_eh) if not slices else {"slices": slices, "estimates": {}}
-        r = tune_split(ctx, acc["slices"])
-        ent = {"tuning": r["tuning"], "slices": acc["slices"],
+        if slices:
+            f = "split_bf16" if form == "split" else form
+            acc = {"form": f, "slices": slices, "estimates": {}}
+        else:
+            acc = choose_slices(ctx, tol_eh, form=form)
+        r = tune_split(ctx, acc["slices"], form=acc["form"])
+        ent = {"tuning": r["tuning"], "form": acc["form"], "slices": acc["slices"],
                "detail": {"accuracy": acc["estimates"], "split": r}}
     ent["seconds"] = time.perf_counter() - t0
     if use_cache:

@@ -18,8 +18,9 @@ EPSI, EPSA, TAI, TABIJ, VABIJ, VIJKA, VABCI, JIJKA, JABCI = range(9)
 TENSOR_IDS = {"epsi": EPSI, "epsa": EPSA, "Tai": TAI, "Tabij": TABIJ, "Vabij": VABIJ,
               "Vijka": VIJKA, "Vabci": VABCI, "Jijka": JIJKA, "Jabci": JABCI}
 # enum atrip_form
-FORM_FP64, FORM_SPLIT_BF16, FORM_AUTO = range(3)
-FORMS = {"fp64": FORM_FP64, "split_bf16": FORM_SPLIT_BF16, "auto": FORM_AUTO}
+FORM_FP64, FORM_SPLIT_BF16, FORM_AUTO, FORM_SPLIT_F16 = range(4)
+FORMS = {"fp64": FORM_FP64, "split_bf16": FORM_SPLIT_BF16, "auto": FORM_AUTO,
+         "split_f16": FORM_SPLIT_F16}
 
 EXPORTED = [
     "atrip_gpu_create", "atrip_gpu_upload", "atrip_gpu_upload_device", "atrip_gpu_release",

@@ -203,7 +203,7 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
   clear_error();
   if (!b || !opts || !results) return fail(ATRIP_ERR_ARGUMENT, "null argument");
   if (opts->form != ATRIP_FORM_FP64 && opts->form != ATRIP_FORM_SPLIT_BF16 &&
-      opts->form != ATRIP_FORM_AUTO)
+      opts->form != ATRIP_FORM_AUTO && opts->form != ATRIP_FORM_SPLIT_F16)
     return fail(ATRIP_ERR_ARGUMENT, "unknown form " + std::to_string(opts->form));
   if (opts->first_iteration < 0 || opts->max_iterations < 0)
     return fail(ATRIP_ERR_ARGUMENT, "negative iteration bound");
@@ -220,7 +220,7 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
   ATRIP_CUDA_TRY(cudaSetDevice(b->device));
   cudaStream_t st = opts->stream ? (cudaStream_t)opts->stream : b->stream;
   const int form = opts->form == ATRIP_FORM_AUTO ? ATRIP_FORM_SPLIT_BF16 : opts->form;
-  const int slices = opts->slices > 0 ? opts->slices : 3;
+  const int slices = opts->slices > 0 ? opts->slices : form == ATRIP_FORM_SPLIT_F16 ? 2 : 3;
   const double tai_sign = opts->ijkabc ? -1.0 : 1.0;
   std::vector<int64_t> prefix;
   fill_table(b, opts->first_iteration, opts->max_iterations, tai_sign, opts->use_j != 0, prefix);
@@ -232,7 +232,7 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
                                 (uintptr_t)prefix[n], (uintptr_t)b->grid,
                                 (uintptr_t)b->tune.fp64_min_blocks,
                                 (uintptr_t)b->tune.tuples_per_claim};
-  if (form == ATRIP_FORM_SPLIT_BF16) {
+  if (form != ATRIP_FORM_FP64) {
     for (int k = 0; k < n; ++k) {
       atrip_gpu_context *c = b->sys[b->order[k]];
       const TriplesArgs &a = b->h_table[k];
@@ -240,6 +240,7 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
       c->split.w_global = c->tune.split_w_global != 0;
       c->split.variant = c->tune.split_variant;
       c->split.prefetch = c->tune.split_prefetch != 0;
+      c->split.f16 = form == ATRIP_FORM_SPLIT_F16;
       int rc = split_prepare(c->split, c->dt, c->No, c->Nv, split_ctas(c), a.use_j != 0, slices,
                              st, &prep_launches);
       if (rc != ATRIP_OK) return rc;

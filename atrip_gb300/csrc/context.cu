@@ -405,7 +405,7 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
     if (!c->have[t])
       return fail(ATRIP_ERR_STATE, "input tensor " + std::to_string(t) + " not uploaded");
   if (opts->form != ATRIP_FORM_FP64 && opts->form != ATRIP_FORM_SPLIT_BF16 &&
-      opts->form != ATRIP_FORM_AUTO)
+      opts->form != ATRIP_FORM_AUTO && opts->form != ATRIP_FORM_SPLIT_F16)
     return fail(ATRIP_ERR_ARGUMENT, "unknown form " + std::to_string(opts->form));
   if (opts->first_iteration < 0 || opts->max_iterations < 0)
     return fail(ATRIP_ERR_ARGUMENT, "negative iteration bound");
@@ -423,7 +423,7 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
                                            : opts->form;
   if (cplx && form != ATRIP_FORM_FP64)
     return fail(ATRIP_ERR_UNSUPPORTED, "complex field: only the FP64 form is built");
-  int slices = opts->slices > 0 ? opts->slices : 3;
+  const int slices = opts->slices > 0 ? opts->slices : form == ATRIP_FORM_SPLIT_F16 ? 2 : 3;
   int64_t launches = 0;
   const uint32_t *order = nullptr;
   if (n > 0 && c->tune.tuple_block > 1) {
@@ -487,6 +487,7 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
       c->split.w_global = c->tune.split_w_global != 0;
       c->split.variant = c->tune.split_variant;
       c->split.prefetch = c->tune.split_prefetch != 0;
+      c->split.f16 = form == ATRIP_FORM_SPLIT_F16;
       const int ctas = c->tune.split_ctas > 0 ? std::min(c->sm_count, (int)c->tune.split_ctas)
                                               : c->sm_count;
       int rc = split_run(c->split, c->dt, c->No, c->Nv, ctas, c->d_tuples, c->d_triples,

@@ -18,6 +18,7 @@ struct SplitState {
   bool w_global = false;    // energy warps read W from L2 even when it fits in smem
   int variant = 0;          // 2: transposed kernel (stacked slices as M) where eligible
   bool prefetch = false;    // L2 prefetch of the next part's slab tiles
+  bool f16 = false;         // FP16 digit slices (radix 2^11) instead of BF16 (2^8)
 };
 
 void split_invalidate(SplitState &s);

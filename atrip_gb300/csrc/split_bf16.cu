@@ -40,6 +40,7 @@
 // buffer sets; every wait is bounded (sm100.cuh).
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
@@ -115,13 +116,15 @@ __global__ void absmax_kernel(const double *__restrict__ x, int64_t n,
   if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
 }
 
-// dst[s][R][k] (pitch Kp, BF16) = sign * digit_s(src(R, k) * scale) for
-// k < K, 0 for K <= k < Kp.  Row R = (o * n1 + r1) * n2 + r2.
+// dst[s][R][k] (pitch Kp) = sign * digit_s(src(R, k) * scale) for k < K,
+// 0 for K <= k < Kp.  Row R = (o * n1 + r1) * n2 + r2.  Digits of radix
+// 2^bits, |q| <= 2^(bits-1): BF16 values for bits = 8, FP16 for bits = 11
+// (integers up to 2^8 and 2^11 are exact in them).
 struct SliceJob {
   const double *src;
   __nv_bfloat16 *dst;
   int64_t nrows, n1, n2, so, s1, s2, sk;
-  int K, Kp, S;
+  int K, Kp, S, bits;
   double scale, sign;
 };
 
@@ -137,10 +140,14 @@ __global__ void slice_kernel(SliceJob j) {
       const int64_t r2 = R % j.n2, t = R / j.n2, r1 = t % j.n1, o = t / j.n1;
       y = j.src[o * j.so + r1 * j.s1 + r2 * j.s2 + k * j.sk] * j.scale;
     }
+    const double radix = j.bits == 11 ? 2048.0 : 256.0;
     for (int s = 0; s < j.S; ++s) {
       const double q = rint(y);
-      j.dst[s * plane + idx] = __double2bfloat16(j.sign * q);
-      y = (y - q) * 256.0;
+      if (j.bits == 11)
+        reinterpret_cast<__half *>(j.dst)[s * plane + idx] = __double2half(j.sign * q);
+      else
+        j.dst[s * plane + idx] = __double2bfloat16(j.sign * q);
+      y = (y - q) * radix;
     }
   }
 }
@@ -265,10 +272,14 @@ __device__ __forceinline__ int energy_rank(int warp, int lane) {
 // epilogue warps fill buffer k % 2 for tuple k while the energy warps read
 // buffer (k-1) % 2, so the tensor-core work of one tuple overlaps the FP64
 // energy evaluation of the previous one.
-template <int S, int NP, bool SPLIT0, bool WSMEM, bool TV, bool MSHARE = false>
+// F16 (transposed variant only): FP16 digits of radix 2^11.  Level 0 is
+// then an FP32 sum of products up to 2^20 -- rounded, not exact, but an
+// integer below 2^31 for K < 2048, so the int32 cell format still holds it.
+template <int S, int NP, bool SPLIT0, bool WSMEM, bool TV, bool MSHARE = false, bool F16 = false>
 __global__ void __launch_bounds__(kThreads, 1)
     triples_split_kernel(const __grid_constant__ SplitMaps maps, const SplitArgs g) {
   using K = typename std::conditional<TV, KernelShapeT<S, MSHARE>, KernelShape<S, NP, SPLIT0>>::type;
+  constexpr float kInvRadix = F16 ? 1.f / 2048.f : 1.f / 256.f;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -508,7 +519,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 // sit side by side in TMEM.  (Transposed variant: the stacked
                 // slices are the M rows, the (p,q) pairs the N columns.)
                 if constexpr (TV) {
-                  const uint32_t id = idesc_bf16_f32(128, g.nmma);
+                  const uint32_t id = F16 ? idesc_f16_f32(128, g.nmma) : idesc_bf16_f32(128, g.nmma);
 #pragma unroll
                   for (int kk = 0; kk < kKChunk / 16; ++kk)
                     if (kk < nkk)
@@ -631,7 +642,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               float rr = 0.f;
 #pragma unroll
               for (int q = S - 1; q >= 1; --q)
-                rr = rr * (1.f / 256.f) + stg[(q * No + r) * kStagePitch + ccu];
+                rr = rr * kInvRadix + stg[(q * No + r) * kStagePitch + ccu];
               const int nq = (int)(((uint32_t)n * mno) >> 20);
               const int f = n - nq * No, sl = q0 + nq;
               int i, jj, kx;
@@ -639,7 +650,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               else if (grp == 1) { i = f; kx = sl; jj = r; }
               else { jj = f; kx = sl; i = r; }
               __stcg(&Wc[i + No * (jj + No * kx)],
-                     make_int2(lev0, __float_as_int(rr * (1.f / 256.f))));
+                     make_int2(lev0, __float_as_int(rr * kInvRadix)));
             }
             named_bar_sync(1, 128);  // the staging buffer is reused
           }
@@ -664,8 +675,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (SPLIT0) lev0[cc] += __float2int_rn(v[S][cc]);
                 float r = 0.f;
 #pragma unroll
-                for (int q = S - 1; q >= 1; --q) r = r * (1.f / 256.f) + v[q][cc];
-                rest[cc] = r * (1.f / 256.f);
+                for (int q = S - 1; q >= 1; --q) r = r * kInvRadix + v[q][cc];
+                rest[cc] = r * kInvRadix;
               }
               // the 16 cells are distinct elements of W: issue every load
               // before any store so the round trips to L2 overlap
@@ -736,10 +747,16 @@ __global__ void __launch_bounds__(kThreads, 1)
       // when it does not fit, written in place over group 0's cells
       const double unit = g.unit;
       double *Wd = WSMEM ? Wsm : Wg;
+      // level-0 parts: each below 2^24 (BF16 digits) or 2^31 (FP16 digits),
+      // so their sum fits int32 or int64 respectively
+      auto lev0 = [](int2 c0, int2 c1, int2 c2) {
+        if constexpr (F16) return (double)((long long)c0.x + c1.x + c2.x);
+        else return (double)(c0.x + c1.x + c2.x);
+      };
       for (int i = er; i < No3; i += kEnergyThreads) {
         const int2 c0 = Wc0[i], c1 = Wc1[i], c2 = Wc2[i];
         const float rest = (__int_as_float(c0.y) + __int_as_float(c1.y)) + __int_as_float(c2.y);
-        Wd[i] = unit * ((double)(c0.x + c1.x + c2.x) + (double)rest);
+        Wd[i] = unit * (lev0(c0, c1, c2) + (double)rest);
       }
       __threadfence_block();
       named_bar_sync(2, kEnergyThreads);
@@ -805,7 +822,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int x = i + No * (j + No * kx);
           const int2 c0 = WJ0[x], c1 = WJ1[x], c2 = WJ2[x];
           const float rest = (__int_as_float(c0.y) + __int_as_float(c1.y)) + __int_as_float(c2.y);
-          return uj * ((double)(c0.x + c1.x + c2.x) + (double)rest);
+          return uj * (lev0(c0, c1, c2) + (double)rest);
         });
       }
       if (er == 0) {
@@ -843,6 +860,7 @@ struct SplitImpl {
   int stage_cap = 0;  // operand ring depth limit (0 = as many as fit)
   bool w_global = false;
   int variant = 0;    // 2: transposed kernel where eligible
+  int bits = 8;       // digit radix 2^bits: 8 = BF16 slices, 11 = FP16 slices
   SplitMaps maps;
 };
 
@@ -928,9 +946,10 @@ int run_slices(SliceJob j, cudaStream_t st) {
   return cudaGetLastError() == cudaSuccess ? ATRIP_OK : ATRIP_ERR_CUDA;
 }
 
-int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, cudaStream_t st,
-            int64_t *launches) {
+int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, int bits,
+            cudaStream_t st, int64_t *launches) {
   p->S = S;
+  p->bits = bits;
   p->No = No;
   p->Nv = Nv;
   p->Ep = (Nv + kKChunk - 1) / kKChunk * kKChunk;
@@ -946,8 +965,10 @@ int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, cudaSt
   *launches += 3;
   const int eT = exponent_of(mT), eV = exponent_of(mVp > mVh ? mVp : mVh);
   p->eT = eT;
-  p->unit = std::ldexp(1.0, eT + eV - 14);
-  const double sT = std::ldexp(1.0, 7 - eT), sV = std::ldexp(1.0, 7 - eV);
+  // x = 2^(e-bits+1) sum_s q_s 2^(-bits s): level-0 products carry
+  // 2^(eT+eV-2(bits-1))
+  p->unit = std::ldexp(1.0, eT + eV - 2 * (bits - 1));
+  const double sT = std::ldexp(1.0, bits - 1 - eT), sV = std::ldexp(1.0, bits - 1 - eV);
 
   const size_t nTa = (size_t)S * Nv * No2 * Ep, nVh = (size_t)S * Nv * No2 * kHoleK,
                nVp = (size_t)S * Nv * Nv * No * Ep, nTp = (size_t)S * Nv * Nv * No * kHoleK;
@@ -963,6 +984,7 @@ int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, cudaSt
   // rows (o, r1, r2) and source strides of each slice tensor
   SliceJob j;
   j.S = S;
+  j.bits = bits;
   j.sign = 1.0;
   // TaS[s][x][q][p][E] = T[x,E,p,q] from Ta[x][q][p][E]
   j.src = dt.Ta; j.dst = p->TaS; j.nrows = Nv * No2; j.n1 = No; j.n2 = No;
@@ -1080,14 +1102,15 @@ int prepare_j(SplitImpl *p, const DeviceTensors &dt, cudaStream_t st, int64_t *l
   if (rc != ATRIP_OK) return rc;
   *launches += 2;
   const int eJ = exponent_of(mJp > mJh ? mJp : mJh);
-  p->unit_j = std::ldexp(1.0, p->eT + eJ - 14);
-  const double sJ = std::ldexp(1.0, 7 - eJ);
+  p->unit_j = std::ldexp(1.0, p->eT + eJ - 2 * (p->bits - 1));
+  const double sJ = std::ldexp(1.0, p->bits - 1 - eJ);
   const size_t nVh = (size_t)S * Nv * No2 * kHoleK, nVp = (size_t)S * Nv * Nv * No * Ep;
   ATRIP_CUDA_TRY(cudaMalloc(&p->JhS, 2 * nVh));
   ATRIP_CUDA_TRY(cudaMalloc(&p->JhST, 2 * nVh));
   ATRIP_CUDA_TRY(cudaMalloc(&p->JpS, 2 * nVp));
   SliceJob j;
   j.S = S;
+  j.bits = p->bits;
   j.sign = 1.0;
   j.src = dt.Jht; j.dst = p->JhS; j.nrows = Nv * No2; j.n1 = No; j.n2 = No;
   j.so = No2 * No; j.s1 = No2; j.s2 = No; j.sk = 1; j.K = No; j.Kp = kHoleK; j.scale = sJ;
@@ -1180,7 +1203,7 @@ size_t mslot_bytes_for(int S, int No) {
   return ((size_t)((S - 1) * No + 128) * 128 + 1023) / 1024 * 1024;
 }
 
-template <int S, bool WSMEM, bool MSHARE>
+template <int S, bool WSMEM, bool MSHARE, bool F16>
 int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   using K = KernelShapeT<S, MSHARE>;
   const size_t No3 = (size_t)a.No * a.No * a.No;
@@ -1199,7 +1222,7 @@ int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t 
   args.nstages = nst;
   args.mslot_bytes = MSHARE ? (int)mslot_bytes_for(S, a.No) : 0;
   const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
-  auto kern = triples_split_kernel<S, 16, false, WSMEM, true, MSHARE>;
+  auto kern = triples_split_kernel<S, 16, false, WSMEM, true, MSHARE, F16>;
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   const int64_t n = a.t_end - a.t_begin;
@@ -1209,15 +1232,16 @@ int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t 
   return ATRIP_OK;
 }
 
-// S slices of No rows fit the 128 M rows, level 0 stays exact (K <= 1024),
+// S slices of No rows fit the 128 M rows, level 0 stays exact (BF16
+// digits, K = 2 (Nv + No) <= 1024) or within int32 (FP16 digits, K < 2048),
 // and two 48 KB operand stages fit next to the singles blocks and staging.
-bool transposed_eligible(int S, int No, int Nv) {
+bool transposed_eligible(int S, int No, int Nv, bool f16 = false) {
   const size_t fixed = 1024 + kTailBytes + kStagingBytes + sizeof(double) * 3 * No * No;
-  return S * No <= 128 && 2 * (Nv + No) <= 1024 &&
+  return S * No <= 128 && 2 * (Nv + No) <= (f16 ? 2047 : 1024) &&
          fixed + 2 * (size_t)KernelShapeT<2>::kStageBytes <= (size_t)kSmemLimit;
 }
 
-template <int S>
+template <int S, bool F16>
 int launch_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   const size_t No3 = (size_t)a.No * a.No * a.No;
   const size_t fixed = 1024 + kTailBytes + kStagingBytes + sizeof(double) * 3 * a.No * a.No;
@@ -1226,18 +1250,28 @@ int launch_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   if (p->variant == 3 && a.No % 8 == 0 &&
       fixed + kMSlots * mslot_bytes_for(S, a.No) + 2 * KernelShapeT<S, true>::kStageBytes <=
           (size_t)kSmemLimit)
-    return launch_shape_t<S, false, true>(p, a, sm_count, st);
+    return launch_shape_t<S, false, true, F16>(p, a, sm_count, st);
   const bool wsmem =
       !p->w_global && fixed + sizeof(double) * No3 + 3 * KernelShapeT<S>::kStageBytes <=
                           (size_t)kSmemLimit;
-  return wsmem ? launch_shape_t<S, true, false>(p, a, sm_count, st)
-               : launch_shape_t<S, false, false>(p, a, sm_count, st);
+  return wsmem ? launch_shape_t<S, true, false, F16>(p, a, sm_count, st)
+               : launch_shape_t<S, false, false, F16>(p, a, sm_count, st);
+}
+
+// FP16 digits: the transposed kernel only (variant 3 where chosen).
+int launch_f16(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
+  if (p->S != 2 || !transposed_eligible(2, a.No, a.Nv, true)) {
+    set_error("split FP16 form: needs 2 slices, No <= 63 and 2 (Nv + No) < 2048 (No=" +
+              std::to_string(a.No) + ", Nv=" + std::to_string(a.Nv) + ")");
+    return ATRIP_ERR_UNSUPPORTED;
+  }
+  return launch_t<2, true>(p, a, sm_count, st);
 }
 
 template <int S>
 int launch_s(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   if (p->variant >= 2 && transposed_eligible(S, a.No, a.Nv))
-    return launch_t<S>(p, a, sm_count, st);
+    return launch_t<S, false>(p, a, sm_count, st);
   const int No = a.No;
   if (No <= 16) return launch_np<S, 16>(p, a, sm_count, st);
   if (No <= 32) return launch_np<S, 32>(p, a, sm_count, st);
@@ -1262,11 +1296,17 @@ int split_prepare(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
     set_error("split form: slices must be 2, 3 or 4");
     return ATRIP_ERR_ARGUMENT;
   }
-  if (!s.valid || s.slices != slices || !s.impl) {
+  const int bits = s.f16 ? 11 : 8;
+  if (s.f16 && slices != 2) {
+    set_error("split FP16 form: slices must be 2");
+    return ATRIP_ERR_ARGUMENT;
+  }
+  if (!s.valid || s.slices != slices || !s.impl ||
+      static_cast<SplitImpl *>(s.impl)->bits != bits) {
     split_free(s);
     auto *p = new SplitImpl();
     s.impl = p;
-    int rc = prepare(p, dt, No, Nv, slices, st, launches);
+    int rc = prepare(p, dt, No, Nv, slices, bits, st, launches);
     if (rc != ATRIP_OK) {
       split_free(s);
       return rc;
@@ -1342,6 +1382,12 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
   a.status = p->d_status;
   a.wglobal = p->wglobal;
   int rc;
+  if (p->bits == 11) {
+    rc = launch_f16(p, a, sm_count, st);
+    if (rc != ATRIP_OK) return rc;
+    *launches += 1;
+    return ATRIP_OK;
+  }
   switch (s.slices) {
     case 2: rc = launch_s<2>(p, a, sm_count, st); break;
     case 3: rc = launch_s<3>(p, a, sm_count, st); break;

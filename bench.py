@@ -3,7 +3,7 @@
 Workloads (synthetic inputs with the benchmark's seeded value distributions):
 
   no40_nv400  (default) No=40, Nv=400, seed 0: the precision workload, on
-              which the benchmark compares the FP64 and split-BF16 forms
+              which the benchmark compares the FP64 and split forms
   no24_nv240  No=24, Nv=240, seed 0 (the plain-FP64 drop-in workload)
   no56_nv560  No=56, Nv=560, seed 0 (the large single system)
   no8_nv40    No=8, Nv=40, seed 0 (the reference's own CPU-sized case)
@@ -18,13 +18,15 @@ Inputs (>= 3 GB) are larger than the 129 MB L2, so no flush is needed.
 
 Metric: FP64-equivalent TFLOP/s of the triples loop (atrip's own count,
 12 No^3 (No + Nv) FLOPs per tuple, src/atrip/Atrip.cxx:578-580), with the
-time to the full E(T) beside it.  The default form is the split-BF16 one
-with its slice count and launch parameters chosen by the autotuner; the
-same line carries the FP64 form's throughput on sample windows of the same
-list and the sampled |dE(T)| between the two forms.
+time to the full E(T) beside it.  The default form ("split") lets the
+autotuner pick the slice format -- 2 FP16 slices where their kernel covers
+the system, else 2..4 BF16 slices -- as the cheapest one whose estimated
+|dE(T)| on the |E(T)| ~ 0.1 Eh twin stays within 1e-8 Eh, then the launch
+parameters; the same line carries the FP64 form's throughput on sample
+windows of the same list and the sampled |dE(T)| between the two forms.
 
-  python bench.py [--workload W] [--form split_bf16|fp64] [--steps K]
-                  [--warmup W] [--impl reference]
+  python bench.py [--workload W] [--form split|split_f16|split_bf16|fp64]
+                  [--steps K] [--warmup W] [--impl reference]
 """
 from __future__ import annotations
 
@@ -125,13 +127,16 @@ def load_peaks():
     return json.load(open(path)) if os.path.exists(path) else {}
 
 
-def traffic_per_tuple(kernel: str, workload: str):
-    """DRAM bytes per tuple of `kernel` on `workload` from the committed ncu
-    summary (profiles/traffic.json), or None."""
+def traffic_per_tuple(kernel: str, workload: str, form: str = "fp64", slices: int = 0):
+    """DRAM bytes per tuple of `kernel` on `workload` in `form` with `slices`
+    from the committed ncu summary (profiles/traffic.json), or None."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
-        t = json.load(open(path))
-        return float(t[kernel][workload]["bytes_per_tuple"])
+        ent = json.load(open(path))[kernel][workload]
+        if kernel == "triples_split_kernel" and (ent.get("form", "split_bf16"),
+                                                 ent.get("slices", 3)) != (form, slices):
+            return None
+        return float(ent["bytes_per_tuple"])
     except (OSError, KeyError, ValueError, TypeError):
         return None
 
@@ -307,14 +312,15 @@ def _roofline(form, slices, flops_per_launch, launch_ms, peaks, live_fp64, traff
     else:
         products = slices * (slices + 1) // 2
         achieved = flops_per_launch * products / (launch_ms * 1e-3) / 1e12
-        peak = peaks.get("bf16_tflops", 1900.0)
+        peak = peaks.get("bf16_tflops", 1900.0)  # FP16 MMAs run at the BF16 rate
         src = ("of measured BF16 dense peak (bf16_tflops, burst)" if "bf16_tflops" in peaks
                else "of fallback BF16 peak")
         kernel = "triples_split_kernel"
     return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": traffic, "peak_source": src, "kernel": kernel,
             "algorithmic": ("FP64-equivalent FLOPs per launch" if form == "fp64" else
-                            f"BF16 MMA FLOPs per launch = FP64-equivalent x S(S+1)/2 = "
+                            f"{'FP16' if form == 'split_f16' else 'BF16'} MMA FLOPs per "
+                            f"launch = FP64-equivalent x S(S+1)/2 = "
                             f"{slices * (slices + 1) // 2} digit products (S={slices}), "
                             "unpadded")}
 
@@ -341,14 +347,16 @@ def run_single(args, workload, world, rank, local):
     ctx = capi.Context(No, Nv, local)
     _upload_all(ctx, d)
     stream = torch.cuda.Stream()
-    if args.tuning:
-        ctx.set_tuning(**json.loads(args.tuning))
-        tune = {"tuning": ctx.get_tuning(), "slices": args.slices or 3}
-    elif args.no_tune:
-        tune = {"tuning": ctx.get_tuning(), "slices": args.slices or 3}
+    if args.tuning or args.no_tune:
+        if args.tuning:
+            ctx.set_tuning(**json.loads(args.tuning))
+        form = "split_bf16" if form == "split" else form
+        tune = {"tuning": ctx.get_tuning(),
+                "slices": args.slices or (2 if form == "split_f16" else 3)}
     else:
         tune = autotune.tune(ctx, form, tol_eh=args.tol_eh, use_cache=not args.retune,
                              slices=args.slices)
+        form = tune.get("form", "split_bf16" if form == "split" else form)
     slices = tune["slices"] if form != "fp64" else 0
 
     def stretch(s):
@@ -381,7 +389,7 @@ def run_single(args, workload, world, rank, local):
         fp64_tune = autotune.tune(ctx, "fp64", use_cache=not args.retune)["tuning"]
         ms64, e64 = autotune.run_windows(ctx, wins, "fp64")
         ctx.set_tuning(**tuned)
-        ms_s, es = autotune.run_windows(ctx, wins, "split_bf16", slices)
+        ms_s, es = autotune.run_windows(ctx, wins, form, slices)
         est = autotune.error_estimate(n, e64, es)
         n_s = est["sample_tuples"]
         fp64_tflops = n_s * fpt / (ms64 * 1e-3) / 1e12
@@ -426,7 +434,7 @@ def run_single(args, workload, world, rank, local):
     # per launch: the steps' mean tuples and mean device time of the loop
     launch_tuples = tuples / len(res)
     kname = "triples_fp64_kernel" if form == "fp64" else "triples_split_kernel"
-    tpt = traffic_per_tuple(kname, workload)
+    tpt = traffic_per_tuple(kname, workload, form, slices)
     roof = _roofline(form, slices, launch_tuples * fpt, kernel_ms, peaks, live_fp64,
                      tpt * launch_tuples if tpt is not None else None)
     roof["tuples_per_launch"] = launch_tuples
@@ -435,7 +443,7 @@ def run_single(args, workload, world, rank, local):
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if form == "fp64" else f"bf16x{slices}->f64",
+        "dtype": "f64" if form == "fp64" else f"{form[6:]}x{slices}->f64",
         "data": "synthetic (seeded, benchmark value distributions)",
         "config": {"workload": f"CCSD(T) triples No={No} Nv={Nv} seed {SEED}", "name": workload,
                    "form": form, "slices": slices, "tuning": tune["tuning"],
@@ -472,7 +480,10 @@ def run_batch96(args, world, rank, local):
         _upload_all(c, d)
         ctxs.append(c)
     form = args.form
-    slices = args.slices or 3
+    if form == "split":  # FP16 slices where every system fits their kernel
+        ok = all(autotune.f16_eligible(c.No, c.Nv) for c in ctxs)
+        form = "split_f16" if ok and args.slices in (0, 2) else "split_bf16"
+    slices = args.slices or (2 if form == "split_f16" else 3)
     tiles = autotune.tune_batch_tiles(ctxs)
     b = capi.Batch(ctxs)
     btune = autotune.tune_batch(b)
@@ -510,7 +521,7 @@ def run_batch96(args, world, rank, local):
     W = 512
     r64 = b.run(form="fp64", use_j=False, max_iterations=W - 1)
     e64 = [c.tuple_energies(0, r.tuples_done)[0].copy() for c, r in zip(ctxs, r64)]
-    rs = b.run(form="split_bf16", slices=slices, use_j=False, max_iterations=W - 1)
+    rs = b.run(form=form, slices=slices, use_j=False, max_iterations=W - 1)
     es = [c.tuple_energies(0, r.tuples_done)[0].copy() for c, r in zip(ctxs, rs)]
     wflops = sum(min(W, capi.n_tuples(Nv)) * flops_per_tuple(No, Nv) for No, Nv, _ in sizes)
     fp64_tflops = wflops / (r64[0].device_ms * 1e-3) / 1e12
@@ -552,7 +563,7 @@ def run_batch96(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if form == "fp64" else f"bf16x{slices}->f64",
+        "dtype": "f64" if form == "fp64" else f"{form[6:]}x{slices}->f64",
         "data": "synthetic (seeded, benchmark value distributions)",
         "config": {"workload": "96 CCSD(T) triples systems, No in [4,20], Nv in [30,200], "
                                "seeds 0..95", "name": "batch96", "form": form, "slices": slices,
@@ -585,7 +596,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
                     choices=sorted(WORKLOADS) + ["custom"])
-    ap.add_argument("--form", default="split_bf16", choices=["fp64", "split_bf16"])
+    ap.add_argument("--form", default="split", choices=["split", "fp64", "split_bf16", "split_f16"],
+                    help="split: the autotuner picks FP16 or BF16 slices and their count")
     ap.add_argument("--slices", type=int, default=0, help="0: chosen by the autotuner")
     ap.add_argument("--tol-eh", type=float, default=1e-8)
     ap.add_argument("--retune", action="store_true", help="ignore the tuning cache")

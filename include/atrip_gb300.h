@@ -68,7 +68,11 @@ enum atrip_form {
   ATRIP_FORM_FP64 = 0,       /* FP64 throughout                               */
   ATRIP_FORM_SPLIT_BF16 = 1, /* operands cut into BF16 slices, tensor cores,  */
                              /* FP32 accumulation, FP64 recombination         */
-  ATRIP_FORM_AUTO = 2        /* the context's tuned choice                    */
+  ATRIP_FORM_AUTO = 2,       /* the context's tuned choice                    */
+  ATRIP_FORM_SPLIT_F16 = 3   /* 2 FP16 slices of 11-bit digits (22 bits per  */
+                             /* operand, the MMAs of 2 BF16 slices); level 0  */
+                             /* FP32-rounded; needs No <= 63 and              */
+                             /* 2 (Nv + No) < 2048                            */
 };
 
 /* Field of the inputs (atrip's Atrip::run<double> / run<Complex>,
@@ -92,7 +96,8 @@ typedef struct {
  * what you need. */
 typedef struct {
   int32_t form;            /* enum atrip_form                                  */
-  int32_t slices;          /* split form: BF16 slices per operand, 2..4 (0: 3) */
+  int32_t slices;          /* split forms: slices per operand, BF16 2..4       */
+                           /* (0: 3), FP16 2 (0: 2)                            */
   int32_t ijkabc;          /* Input::ijkabc: negate T1, skip final negation    */
   int32_t use_j;           /* 1: (cT) with JIJKA/JABCI when both uploaded      */
   int64_t first_iteration; /* resume cursor (checkpoint Iteration)             */

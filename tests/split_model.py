@@ -3,7 +3,8 @@
 The split form writes each FP64 element as 2^(e-7) sum_p q_p 2^(-8p) with
 integer digits |q_p| <= 128 (one power-of-two scale per tensor: 2^eT for T,
 2^eV shared by V_pphp and V_hhhp), and keeps the digit products of level
-p + q < S.  Because the doubles contribution is bilinear in (T, V), the kept
+p + q < S.  The FP16 form does the same with radix 2^11 (bits=11):
+2^(e-10) sum_p q_p 2^(-11p), |q_p| <= 1024.  Because the doubles contribution is bilinear in (T, V), the kept
 sum equals
 
     W_S = sum_{p < S} doubles(T_p, V_{< S-p}),
@@ -26,15 +27,16 @@ def exponent(maxabs: float) -> int:
     return 0 if maxabs <= 0 else math.frexp(maxabs)[1]  # maxabs < 2^e
 
 
-def digit_components(x: np.ndarray, e: int, S: int):
-    """[x_0, ..., x_{S-1}]: x_p = q_p 2^(e-7-8p)."""
-    y = np.ldexp(np.asarray(x, dtype=np.float64), 7 - e)
+def digit_components(x: np.ndarray, e: int, S: int, bits: int = 8):
+    """[x_0, ..., x_{S-1}]: x_p = q_p 2^(e-(bits-1)-bits p)."""
+    h = bits - 1
+    y = np.ldexp(np.asarray(x, dtype=np.float64), h - e)
     out = []
     for p in range(S):
         q = np.rint(y)
-        assert np.max(np.abs(q)) <= 128
-        out.append(np.ldexp(q, e - 7 - 8 * p))
-        y = (y - q) * 256.0
+        assert np.max(np.abs(q)) <= 2 ** h
+        out.append(np.ldexp(q, e - h - bits * p))
+        y = (y - q) * 2.0 ** bits
     return out
 
 
@@ -51,21 +53,21 @@ def _problems(d, Tc, Pc, Hc, S, pkey, hkey):
 
 
 def split_tuple_energies(d: dict, S: int, t0: int = 0, t1: int | None = None,
-                         use_j: bool = False):
-    """Per-tuple energies of the split form's arithmetic with S slices;
-    with use_j also the (cT) energies (T from the J intermediates, Z from
-    V), returned as (e, ect)."""
+                         use_j: bool = False, bits: int = 8):
+    """Per-tuple energies of the split form's arithmetic with S slices of
+    radix 2^bits (8: BF16 form, 11: FP16 form); with use_j also the (cT)
+    energies (T from the J intermediates, Z from V), returned as (e, ect)."""
     No, Nv = d["No"], d["Nv"]
     eT = exponent(float(np.max(np.abs(d["Tabij"]))))
     eV = exponent(max(float(np.max(np.abs(d["Vabci"]))), float(np.max(np.abs(d["Vijka"])))))
-    Tc = digit_components(d["Tabij"], eT, S)
-    problems = _problems(d, Tc, digit_components(d["Vabci"], eV, S),
-                         digit_components(d["Vijka"], eV, S), S, "Vabci", "Vijka")
+    Tc = digit_components(d["Tabij"], eT, S, bits)
+    problems = _problems(d, Tc, digit_components(d["Vabci"], eV, S, bits),
+                         digit_components(d["Vijka"], eV, S, bits), S, "Vabci", "Vijka")
     jproblems = []
     if use_j:
         eJ = exponent(max(float(np.max(np.abs(d["Jabci"]))), float(np.max(np.abs(d["Jijka"])))))
-        jproblems = _problems(d, Tc, digit_components(d["Jabci"], eJ, S),
-                              digit_components(d["Jijka"], eJ, S), S, "Jabci", "Jijka")
+        jproblems = _problems(d, Tc, digit_components(d["Jabci"], eJ, S, bits),
+                              digit_components(d["Jijka"], eJ, S, bits), S, "Jabci", "Jijka")
     full = oracle.Problem(d)
     lst = oracle.tuple_list(Nv)
     t1 = len(lst) if t1 is None else t1

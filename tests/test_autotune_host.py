@@ -43,3 +43,18 @@ def test_error_estimate_extrapolates_and_scales_the_twin():
     # ijkabc keeps atrip's accumulated sign
     est2 = autotune.error_estimate(n, ref, test, ijkabc=True)
     assert math.isclose(est2["dE_est"], n * delta, rel_tol=1e-6)
+
+
+def test_split_formats_order_and_eligibility():
+    # FP16 2 slices first where its kernel covers the system; BF16 2 slices
+    # (same digit products, fewer bits) then drop out
+    assert autotune.split_formats(40, 400) == [("split_f16", 2), ("split_bf16", 3),
+                                               ("split_bf16", 4)]
+    assert autotune.split_formats(40, 400, "split_bf16") == [("split_bf16", 2), ("split_bf16", 3),
+                                                             ("split_bf16", 4)]
+    assert autotune.split_formats(40, 400, "split_f16") == [("split_f16", 2)]
+    # No > 63 (shared memory), or K = 2 (Nv + No) >= 2048: BF16 only
+    assert autotune.split_formats(64, 100)[0] == ("split_bf16", 2)
+    assert autotune.split_formats(20, 1004)[0] == ("split_bf16", 2)
+    assert autotune.f16_eligible(56, 560) and autotune.f16_eligible(63, 960)
+    assert not autotune.f16_eligible(63, 961)

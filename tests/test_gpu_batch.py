@@ -48,7 +48,7 @@ def _singles(ctxs, **kw):
     return out
 
 
-@pytest.mark.parametrize("form", ["fp64", "split_bf16"])
+@pytest.mark.parametrize("form", ["fp64", "split_bf16", "split_f16"])
 @pytest.mark.parametrize("ijkabc", [False, True])
 def test_batch_matches_single_runs(systems, form, ijkabc):
     ds, ctxs = systems

@@ -8,13 +8,18 @@ Two references:
 * the FP64 form: the error of the split form itself, bounded per slice count
   (S=2: 1e-4, S=3: 1e-6, S=4: 1e-8 relative per tuple), and the benchmark's
   |dE(T)| <= 1e-8 Eh on a power-of-two-scaled twin with |E(T)| ~ 0.1 Eh.
+
+The FP16 form (2 slices of 11-bit digits) rounds its level-0 sums in FP32
+(products up to 2^20 do not stay exact), so its bar against the model is
+the FP32 rounding of level 0: 3e-6 relative per tuple; against the FP64
+form 5e-6 (its digit truncation alone gives ~1e-6).
 """
 import numpy as np
 import pytest
 
 import oracle
 import split_model
-from atrip_gb300 import capi, synth
+from atrip_gb300 import autotune, capi, synth
 
 pytestmark = pytest.mark.gpu
 BOUND = {2: 1e-4, 3: 1e-6, 4: 1e-8}
@@ -179,3 +184,108 @@ def test_transposed_variant_with_j_and_knobs(No, Nv, seed, S):
             s = np.max(np.abs(e1))
             assert np.max(np.abs(e2 - e1)) <= 1e-9 * s, (tune, np.max(np.abs(e2 - e1)) / s)
             assert np.max(np.abs(c2 - c1)) <= 1e-9 * s, tune
+
+
+F16_MODEL_TOL, F16_BOUND = 3e-6, 5e-6
+
+
+@pytest.mark.parametrize("No,Nv,seed", CASES)
+@pytest.mark.parametrize("variant", [2, 3])
+def test_f16_matches_model_and_fp64(No, Nv, seed, variant):
+    d = synth.make_inputs(No, Nv, seed)
+    n = min(synth.n_tuples(Nv), 120)
+    if not autotune.f16_eligible(No, Nv):
+        with _ctx(d) as ctx, pytest.raises(capi.AtripError) as ei:
+            ctx.run(form="split_f16", use_j=False, max_iterations=n - 1)
+        assert ei.value.status == capi.ERR_UNSUPPORTED
+        return
+    model = split_model.split_tuple_energies(d, 2, 0, n, bits=11)
+    with _ctx(d) as ctx:
+        r64 = ctx.run(form="fp64", use_j=False, max_iterations=n - 1)
+        e64, _ = ctx.tuple_energies(0, n)
+        ctx.set_tuning(split_variant=variant)
+        r = ctx.run(form="split_f16", use_j=False, max_iterations=n - 1)
+        assert r.form_used == capi.FORM_SPLIT_F16 and r.slices_used == 2
+        e, ect = ctx.tuple_energies(0, n)
+    assert np.array_equal(e, ect)
+    if No == 1:
+        assert np.max(np.abs(e)) <= 1e-12
+        return
+    scale = np.max(np.abs(model))
+    assert np.max(np.abs(e - model)) <= F16_MODEL_TOL * scale, np.max(np.abs(e - model)) / scale
+    rel = np.max(np.abs(e - e64)) / np.max(np.abs(e64))
+    assert rel <= F16_BOUND, rel
+    assert abs(r.energy - r64.energy) <= F16_BOUND * abs(r64.energy)
+
+
+def test_f16_scaled_twin_meets_1e8_hartree():
+    d0 = synth.make_inputs(8, 40, 0)
+    with _ctx(d0) as ctx:
+        e0 = ctx.run(form="fp64", use_j=False).energy
+    k = int(round(np.log2(abs(e0) / 0.1) / 4))
+    d = synth.make_inputs(8, 40, 0, scale=2.0 ** -k)
+    with _ctx(d) as ctx:
+        e64 = ctx.run(form="fp64", use_j=False).energy
+        e2 = ctx.run(form="split_f16", use_j=False).energy
+    assert 0.01 < abs(e64) < 1.0
+    assert abs(e2 - e64) <= 1e-8, abs(e2 - e64)
+
+
+@pytest.mark.parametrize("No,Nv,seed", [(5, 9, 3), (8, 20, 1), (24, 14, 2), (32, 12, 6)])
+def test_f16_ct_energy_and_knobs(No, Nv, seed):
+    """(cT) pass against the model; ring depth, W placement, variant 3 and
+    the blocked order change the schedule only (1e-9 relative)."""
+    d = synth.make_inputs(No, Nv, seed, with_j=True)
+    n = min(synth.n_tuples(Nv), 80)
+    model_e, model_ct = split_model.split_tuple_energies(d, 2, 0, n, use_j=True, bits=11)
+    with _ctx(d) as ctx:
+        ctx.upload("Jijka", d["Jijka"])
+        ctx.upload("Jabci", d["Jabci"])
+        r64 = ctx.run(form="fp64", use_j=True, max_iterations=n - 1)
+        ctx.run(form="split_f16", use_j=True, max_iterations=n - 1)
+        e, ect = ctx.tuple_energies(0, n)
+        scale = np.max(np.abs(model_e))
+        assert np.max(np.abs(e - model_e)) <= F16_MODEL_TOL * scale
+        assert np.max(np.abs(ect - model_ct)) <= F16_MODEL_TOL * scale
+        for tune in ({"split_variant": 3}, {"split_w_global": 1}, {"split_stages": 2},
+                     {"split_variant": 3, "tuple_block": 4}, {"split_prefetch": 1}):
+            ctx.set_tuning(**tune)
+            r = ctx.run(form="split_f16", use_j=True, max_iterations=n - 1)
+            e2, c2 = ctx.tuple_energies(0, n)
+            assert np.max(np.abs(e2 - e)) <= 1e-9 * scale, tune
+            assert np.max(np.abs(c2 - ect)) <= 1e-9 * scale, tune
+        assert abs(r.ct_energy - r64.ct_energy) <= F16_BOUND * abs(r64.energy)
+        # switching back to BF16 slices re-cuts the operands
+        ctx.set_tuning(split_variant=2)
+        rb = ctx.run(form="split_bf16", slices=3, use_j=True, max_iterations=n - 1)
+        assert rb.form_used == capi.FORM_SPLIT_BF16
+        assert abs(rb.energy - r64.energy) <= BOUND[3] * abs(r64.energy)
+
+
+def test_f16_large_k():
+    """K = 2 (Nv + No) = 1036 > 1024: beyond the BF16 transposed kernel,
+    within the FP16 one (level 0 < 2^31)."""
+    No, Nv = 3, 515
+    d = synth.make_inputs(No, Nv, 11)
+    n = 256
+    with _ctx(d) as ctx:
+        ctx.run(form="fp64", max_iterations=n - 1)
+        e64, _ = ctx.tuple_energies(0, n)
+        ctx.run(form="split_f16", max_iterations=n - 1)
+        e, _ = ctx.tuple_energies(0, n)
+    assert np.max(np.abs(e - e64)) / np.max(np.abs(e64)) <= 1e-5
+
+
+def test_f16_rejects_what_it_does_not_cover():
+    d = synth.make_inputs(4, 7, 1)
+    with _ctx(d) as ctx:
+        with pytest.raises(capi.AtripError) as ei:
+            ctx.run(form="split_f16", slices=3)
+        assert ei.value.status == capi.ERR_ARGUMENT
+        assert np.isfinite(ctx.run(form="split_f16").energy)
+    d = synth.make_inputs(64, 4, 2)  # two operand stages do not fit beside the singles
+    with _ctx(d) as ctx:
+        with pytest.raises(capi.AtripError) as ei:
+            ctx.run(form="split_f16")
+        assert ei.value.status == capi.ERR_UNSUPPORTED
+        assert np.isfinite(ctx.run(form="split_bf16", slices=2).energy)

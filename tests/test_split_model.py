@@ -1,0 +1,34 @@
+"""CPU checks of the split-precision digit model (no GPU): digit bounds,
+exact reconstruction, and the truncation error of each slice format against
+the FP64 oracle, which sets the bars the GPU split tests use."""
+import numpy as np
+import pytest
+
+import oracle
+import split_model
+from atrip_gb300 import synth
+
+
+@pytest.mark.parametrize("bits", [8, 11])
+def test_digits_bounded_and_exact(bits):
+    rng = np.random.default_rng(bits)
+    x = rng.standard_normal(4096) * np.exp(rng.uniform(-20, 0, 4096))
+    e = split_model.exponent(float(np.max(np.abs(x))))
+    comps = split_model.digit_components(x, e, 8, bits)  # asserts |q| <= 2^(bits-1)
+    # 8 digits carry at least 64 bits: the sum reproduces x to FP64 rounding
+    assert np.max(np.abs(sum(comps) - x)) <= 4 * np.finfo(float).eps * np.max(np.abs(x))
+    # digit p carries radix^-p of the scale: the partial sums converge
+    for S in range(1, 4):
+        err = np.max(np.abs(sum(comps[:S]) - x))
+        assert err <= 2.0 ** (e - (bits - 1) - bits * (S - 1) - 1), (S, err)
+
+
+@pytest.mark.parametrize("S,bits,bound", [(2, 8, 1e-4), (3, 8, 1e-6), (2, 11, 5e-6)])
+def test_model_truncation_error(S, bits, bound):
+    for No, Nv, seed in [(8, 40, 0), (13, 17, 2)]:
+        d = synth.make_inputs(No, Nv, seed)
+        n = 60
+        e = split_model.split_tuple_energies(d, S, 0, n, bits=bits)
+        e64, _ = oracle.tuple_energies(oracle.Problem(d), 0, n, use_j=False)
+        rel = np.max(np.abs(e - e64)) / np.max(np.abs(e64))
+        assert rel <= bound, (No, Nv, rel)
