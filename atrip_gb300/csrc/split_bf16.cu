@@ -712,6 +712,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ------------------------------------------------ energy (10 warps)
     const int er = energy_rank(warp, lane);
     const int64_t Nv = g.Nv;
+    // W, Z and the singles are carried in units of unit (W cell = level-0
+    // integer + rest), the (cT) T in units of unit_j; both are powers of
+    // two, so the tuple energies scale back exactly at the end
+    const double inv_unit = 1.0 / g.unit;
     for (uint32_t k = 0;; ++k) {
       const int ts = k % kTupleSlots;
       bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull);
@@ -721,9 +725,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!ok || s.t < 0) break;
       const int a = s.a, b = s.b, c = s.c;
       if (er < No) {
-        ta[er] = g.tai_sign * g.tai[a + er * Nv];
-        tb[er] = g.tai_sign * g.tai[b + er * Nv];
-        tc[er] = g.tai_sign * g.tai[c + er * Nv];
+        // in units of the W cells (a power of two: exact)
+        ta[er] = g.tai_sign * g.tai[a + er * Nv] * inv_unit;
+        tb[er] = g.tai_sign * g.tai[b + er * Nv] * inv_unit;
+        tc[er] = g.tai_sign * g.tai[c + er * Nv] * inv_unit;
       }
       {
         const double *Vbc = g.Vhh + ((int64_t)b * Nv + c) * No2;
@@ -741,11 +746,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       double *Wg = Wbase + (size_t)(wb * npass) * 3 * No3;
       const int2 *Wc0 = reinterpret_cast<const int2 *>(Wg);
       const int2 *Wc1 = Wc0 + No3, *Wc2 = Wc1 + No3;
-      // W = unit * (level-0 integer + rest) in FP64 from the three group
+      // W / unit = level-0 integer + rest in FP64 from the three group
       // cells (integer parts exact, rests added in group order): copied into
       // shared memory (the buffers go back to the epilogue at once), or,
       // when it does not fit, written in place over group 0's cells
-      const double unit = g.unit;
       double *Wd = WSMEM ? Wsm : Wg;
       // level-0 parts: each below 2^24 (BF16 digits) or 2^31 (FP16 digits),
       // so their sum fits int32 or int64 respectively
@@ -753,10 +757,28 @@ __global__ void __launch_bounds__(kThreads, 1)
         if constexpr (F16) return (double)((long long)c0.x + c1.x + c2.x);
         else return (double)(c0.x + c1.x + c2.x);
       };
-      for (int i = er; i < No3; i += kEnergyThreads) {
-        const int2 c0 = Wc0[i], c1 = Wc1[i], c2 = Wc2[i];
-        const float rest = (__int_as_float(c0.y) + __int_as_float(c1.y)) + __int_as_float(c2.y);
-        Wd[i] = unit * (lev0(c0, c1, c2) + (double)rest);
+      // four elements per thread in flight: the cells come from L2
+      constexpr int kU = 4;
+      for (int i0 = er; i0 < No3; i0 += kU * kEnergyThreads) {
+        int2 c[kU][3];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int i = i0 + u * kEnergyThreads;
+          if (i < No3) {
+            c[u][0] = Wc0[i];
+            c[u][1] = Wc1[i];
+            c[u][2] = Wc2[i];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int i = i0 + u * kEnergyThreads;
+          if (i < No3) {
+            const float rest = (__int_as_float(c[u][0].y) + __int_as_float(c[u][1].y)) +
+                               __int_as_float(c[u][2].y);
+            Wd[i] = lev0(c[u][0], c[u][1], c[u][2]) + (double)rest;
+          }
+        }
       }
       __threadfence_block();
       named_bar_sync(2, kEnergyThreads);
@@ -811,18 +833,17 @@ __global__ void __launch_bounds__(kThreads, 1)
         named_bar_sync(2, kEnergyThreads);  // red is reused
         return e;
       };
-      const double e = tuple_energy(W);
+      const double e = (g.unit * g.unit) * tuple_energy(W);
       double ect = e;
       if (g.use_j) {
         // (cT): T from the J pass, Z as above (src/atrip/Atrip.cxx:928-963)
         const int2 *WJ0 = reinterpret_cast<const int2 *>(Wbase + (size_t)(wb * npass + 1) * 3 * No3);
         const int2 *WJ1 = WJ0 + No3, *WJ2 = WJ1 + No3;
-        const double uj = g.unit_j;
-        ect = tuple_energy([&](int i, int j, int kx) {
+        ect = (g.unit * g.unit_j) * tuple_energy([&](int i, int j, int kx) {
           const int x = i + No * (j + No * kx);
           const int2 c0 = WJ0[x], c1 = WJ1[x], c2 = WJ2[x];
           const float rest = (__int_as_float(c0.y) + __int_as_float(c1.y)) + __int_as_float(c2.y);
-          return uj * (lev0(c0, c1, c2) + (double)rest);
+          return lev0(c0, c1, c2) + (double)rest;
         });
       }
       if (er == 0) {
