@@ -18,9 +18,9 @@
 //    would write one every iteration (checkpoint modulus 0,
 //    src/atrip/Atrip.cxx:588-591, 713) they are written between tuple chunks
 //    of the device queue (checkpoint_chunks per run);
-//  * extra attributes select the arithmetic form and device (form, slices,
-//    device);
-//  * F = std::complex<double> is declared but throws: not built yet.
+//  * extra attributes select the arithmetic form and device (form: an
+//    atrip_form value -- FP64, BF16 or FP16 split, auto; slices; device);
+//  * F = std::complex<double> runs the FP64 form only.
 #ifndef ATRIP_GB300_ATRIP_HPP_
 #define ATRIP_GB300_ATRIP_HPP_
 
