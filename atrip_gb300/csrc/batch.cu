@@ -242,7 +242,7 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
       c->split.prefetch = c->tune.split_prefetch != 0;
       c->split.f16 = form == ATRIP_FORM_SPLIT_F16;
       int rc = split_prepare(c->split, c->dt, c->No, c->Nv, split_ctas(c), a.use_j != 0, slices,
-                             st, &prep_launches);
+                             a.triples, a.n_triples, st, &prep_launches);
       if (rc != ATRIP_OK) return rc;
       const uintptr_t more[] = {(uintptr_t)c->split.generation, (uintptr_t)c->split.impl,
                                 (uintptr_t)a.epsi, (uintptr_t)a.epsa, (uintptr_t)a.tai,

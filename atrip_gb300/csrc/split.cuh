@@ -26,7 +26,8 @@ void split_free(SplitState &s);
 
 // Cut the digit slices and build the tensor maps (host work, allocations).
 int split_prepare(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
-                  bool use_j, int slices, cudaStream_t st, int64_t *launches);
+                  bool use_j, int slices, const uint32_t *triples, int n_triples,
+                  cudaStream_t st, int64_t *launches);
 // Queue one launch over tuples [t_begin, t_end) on st (no host sync; may be
 // captured into a CUDA graph).  The caller zeroes *queue first.
 int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,

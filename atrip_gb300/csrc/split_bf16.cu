@@ -92,6 +92,7 @@ struct SplitArgs {
   int nstages;                 // operand ring depth
   const double *epsi, *epsa, *tai, *Vhh;
   const uint32_t *tuples, *triples;
+  const double2 *tri_ef;  // per (i,j,k) triple: (e_i + e_j) + e_k, 2 fac_jk fac_ij
   int n_triples;
   int64_t t_begin, t_end;
   const uint32_t *order;  // queue slot q runs list position t_begin + order[q]
@@ -114,6 +115,37 @@ __global__ void absmax_kernel(const double *__restrict__ x, int64_t n,
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// Per (i,j,k) triple of the energy loop, independent of the tuple: the
+// occupied-orbital part of the denominator, summed as the loop summed it,
+// and the weight 2 fac_jk fac_ij of src/atrip/Equations.cxx:101-238 (both
+// factors 1/2 on equal indices; a power of two, so applying it to the
+// reciprocal instead of the quotient is exact).
+__global__ void triple_table_kernel(const uint32_t *__restrict__ triples, int n,
+                                    const double *__restrict__ epsi, double2 *__restrict__ out) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const uint32_t tp = triples[t];
+    const int i = tp & 0xff, j = (tp >> 8) & 0xff, k = (tp >> 16) & 0xff;
+    const double fac = (j == k ? 0.5 : 1.0) * (i == j ? 0.5 : 1.0);
+    out[t] = make_double2((epsi[i] + epsi[j]) + epsi[k], 2.0 * fac);
+  }
+}
+
+__device__ __noinline__ double recip_div(double d) { return 1.0 / d; }
+
+// 1/d for the energy denominators: the FP32 reciprocal of d refined by one
+// Newton-Raphson step, x1 = x0 + x0 (1 - d x0).  With |x0 d - 1| <= ~2^-23
+// the relative error of x1 is about its square (< 2^-44) plus one rounding;
+// outside the FP32 range it falls back to the division (out of line: the
+// orbital-energy gaps never get there).
+__device__ __forceinline__ double recip_nr(double d) {
+  const float df = __double2float_rn(d);
+  const float ad = fabsf(df);
+  if (!(ad > 1e-30f && ad < 1e30f)) return recip_div(d);
+  const double x0 = (double)__frcp_rn(df);
+  const double e = fma(-d, x0, 1.0);
+  return fma(x0, e, x0);
 }
 
 // dst[s][R][k] (pitch Kp) = sign * digit_s(src(R, k) * scale) for k < K,
@@ -310,8 +342,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   double *tb = ta + 64;
   double *tc = tb + 64;
   double *red = tc + 64;        // [kEnergyWarps]
-  double *esm = red + 16;       // eps_i
-  double *Vsm = esm + 64;       // 3 No x No blocks for the singles
+  double *Vsm = red + 16 + 64;  // 3 No x No blocks for the singles
   double *Wsm = Vsm + 3 * No2;  // FP64 copy of W for the energy loop (WSMEM)
   float *stg = reinterpret_cast<float *>(Wsm + (WSMEM ? No3 : 0));  // TV epilogue staging
 
@@ -740,7 +771,6 @@ __global__ void __launch_bounds__(kThreads, 1)
           Vsm[2 * No2 + i] = Vab[i];
         }
       }
-      if (er < No) esm[er] = g.epsi[er];
       const int wb = k & 1;
       ok = mbar_wait(&wfull[wb], (k >> 1) & 1, g.status, kErrTimeoutAccFull);
       double *Wg = Wbase + (size_t)(wb * npass) * 3 * No3;
@@ -804,9 +834,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         double sum = 0.0;
         for (int n = er; n < g.n_triples && ok; n += kEnergyThreads) {
           const uint32_t tp = g.triples[n];
+          const double2 ef = g.tri_ef[n];
           const int i = tp & 0xff, j = (tp >> 8) & 0xff, kx = (tp >> 16) & 0xff;
-          const double facjk = j == kx ? 0.5 : 1.0, facij = i == j ? 0.5 : 1.0;
-          const double denominator = epsabc - ((esm[i] + esm[j]) + esm[kx]);
+          const double denominator = epsabc - ef.x;
           double value;
           if (distinct) {
             const double U = Zv(i, j, kx), V = Zv(i, kx, j), Wv = Zv(j, i, kx),
@@ -822,7 +852,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const double A = Tv(i, j, kx), B = Tv(j, kx, i), C = Tv(kx, i, j);
             value = 3.0 * ((A * U + B * V) + C * Wv) - (A + (B + C)) * (U + (V + Wv));
           }
-          sum += (2.0 * value / denominator) * (facjk * facij);
+          sum = fma(value, recip_nr(denominator) * ef.y, sum);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
@@ -882,6 +912,8 @@ struct SplitImpl {
   bool w_global = false;
   int variant = 0;    // 2: transposed kernel where eligible
   int bits = 8;       // digit radix 2^bits: 8 = BF16 slices, 11 = FP16 slices
+  double2 *tri_ef = nullptr;  // per-triple denominator part and weight
+  int tri_n = 0;
   SplitMaps maps;
 };
 
@@ -899,6 +931,7 @@ void free_impl(SplitImpl *p) {
   cudaFree(p->JpS);
   cudaFree(p->wglobal);
   cudaFree(p->d_status);
+  cudaFree(p->tri_ef);
   delete p;
 }
 
@@ -1312,7 +1345,8 @@ void split_free(SplitState &s) {
 }
 
 int split_prepare(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
-                  bool use_j, int slices, cudaStream_t st, int64_t *launches) {
+                  bool use_j, int slices, const uint32_t *triples, int n_triples,
+                  cudaStream_t st, int64_t *launches) {
   if (slices < 2 || slices > 4) {
     set_error("split form: slices must be 2, 3 or 4");
     return ATRIP_ERR_ARGUMENT;
@@ -1328,6 +1362,18 @@ int split_prepare(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
     auto *p = new SplitImpl();
     s.impl = p;
     int rc = prepare(p, dt, No, Nv, slices, bits, st, launches);
+    if (rc == ATRIP_OK && n_triples > 0) {
+      if (cudaMalloc(&p->tri_ef, sizeof(double2) * n_triples) != cudaSuccess) {
+        set_error("split form: allocating the triple table failed");
+        rc = ATRIP_ERR_CUDA;
+      } else {
+        triple_table_kernel<<<(n_triples + 255) / 256, 256, 0, st>>>(triples, n_triples,
+                                                                     dt.epsi, p->tri_ef);
+        rc = cudaGetLastError() == cudaSuccess ? ATRIP_OK : ATRIP_ERR_CUDA;
+        p->tri_n = n_triples;
+        *launches += 1;
+      }
+    }
     if (rc != ATRIP_OK) {
       split_free(s);
       return rc;
@@ -1368,6 +1414,10 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
     set_error("split form: W buffers prepared for fewer CTAs");
     return ATRIP_ERR_STATE;
   }
+  if (p->tri_n != n_triples) {
+    set_error("split form: triple table prepared for another list");
+    return ATRIP_ERR_STATE;
+  }
   p->stage_cap = s.stage_cap;
   p->w_global = s.w_global;
   p->variant = s.variant;
@@ -1389,6 +1439,7 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
   a.Vhh = dt.Vhh;
   a.tuples = tuples;
   a.triples = triples;
+  a.tri_ef = p->tri_ef;
   a.n_triples = n_triples;
   a.t_begin = t_begin;
   a.t_end = t_end;
@@ -1437,7 +1488,8 @@ int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_cou
               int64_t t_end, const uint32_t *order, double tai_sign, bool use_j, int slices,
               unsigned long long *queue, double *e, double *ect, cudaStream_t st,
               int64_t *launches) {
-  int rc = split_prepare(s, dt, No, Nv, sm_count, use_j, slices, st, launches);
+  int rc = split_prepare(s, dt, No, Nv, sm_count, use_j, slices, triples, n_triples, st,
+                         launches);
   if (rc != ATRIP_OK) return rc;
   rc = split_enqueue(s, dt, No, Nv, sm_count, tuples, triples, n_triples, t_begin, t_end, order,
                      tai_sign, use_j, queue, e, ect, st, launches);
