@@ -47,7 +47,7 @@ static int drive(const std::string &dir, int No, int Nv, int hasJ, int form) {
                 .with_Vabci(Vabci)
                 .with_read_checkpoint_if_exists(false)
                 .with_form(form)
-                .with_slices(3);
+                .with_slices(form == ATRIP_FORM_SPLIT_F16 ? 2 : 3);
   if (hasJ)
     in.with_Jijka(tensor<F>({No, No, No, Nv}, load<F>(dir, "Jijka", o * o * o * v)))
         .with_Jabci(tensor<F>({Nv, Nv, Nv, No}, load<F>(dir, "Jabci", v * v * v * o)));

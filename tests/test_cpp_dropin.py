@@ -1,6 +1,6 @@
 """atrip's C++ API through the drop-in header (include/atrip.hpp): compiles
 against the MPI/CTF stand-ins without a GPU; runs on the GPU and matches
-the oracle (FP64 form at 1e-10, split form within its 3-slice bound, the
+the oracle (FP64 form at 1e-10, split forms within their bounds, the
 complex field's FP64 form at 1e-10)."""
 import os
 import subprocess
@@ -31,9 +31,10 @@ def test_dropin_header_compiles(tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("form,tol,field", [(0, 1e-10, "real"), (1, 1e-6, "real"),
-                                            (0, 1e-10, "complex")])
+                                            (3, 5e-6, "real"), (0, 1e-10, "complex")])
 def test_dropin_runs_and_matches_oracle(tmp_path, form, tol, field):
-    """run<double> in both forms and run<Complex> (FP64 form)."""
+    """run<double> in the FP64 form and the two split forms (BF16, 3 slices;
+    FP16, 2 slices) and run<Complex> (FP64 form)."""
     exe = build_driver(str(tmp_path))
     d = synth.make_inputs(6, 11, 2, with_j=True, field=field)
     data = str(tmp_path / "in")

@@ -191,18 +191,18 @@ def test_chunked_host_upload_matches(tmp_path):
     assert res[""] == res["97"], res
 
 
-@pytest.mark.parametrize("form", ["fp64", "split_bf16"])
-def test_blocked_order_leaves_results_unchanged(form):
+@pytest.mark.parametrize("form,slices", [("fp64", 0), ("split_bf16", 3), ("split_f16", 2)])
+def test_blocked_order_leaves_results_unchanged(form, slices):
     """tuple_block only changes the order in which the work queue hands out
     tuples: per-tuple energies (indexed by list position) and totals stay
     the same, also for a range that starts and ends inside a block."""
     d = synth.make_inputs(7, 23, 4)
     with _ctx_for(d) as ctx:
-        ref = ctx.run(form=form, slices=3, first_iteration=37, max_iterations=1200)
+        ref = ctx.run(form=form, slices=slices, first_iteration=37, max_iterations=1200)
         e_ref, _ = ctx.tuple_energies(37, ref.tuples_done)
         for L in (2, 5, 8):
             ctx.set_tuning(tuple_block=L)
-            r = ctx.run(form=form, slices=3, first_iteration=37, max_iterations=1200)
+            r = ctx.run(form=form, slices=slices, first_iteration=37, max_iterations=1200)
             e, _ = ctx.tuple_energies(37, r.tuples_done)
             assert np.array_equal(e, e_ref), L
             assert abs(r.energy - ref.energy) <= 1e-13 * abs(ref.energy)
