@@ -5,8 +5,7 @@ Runs the reference's OWN sources, compiled one-rank with the shims in
 (``atrip_gb300.synth``) and records:
 
 * ``Atrip::run`` totals (energy, ct_energy) -- with GROUP_AND_SORT, because
-  the NAIVE distribution throws in the slice bookkeeping at one rank (see
-  the oracle notes in DESIGN.md);
+  the NAIVE distribution throws in the slice bookkeeping at one rank;
 * per-tuple energies from the reference's doubles_contribution /
   singles_contribution / get_energy_* called tuple by tuple;
 * Tijk / Zijk of one tuple at a tiny size.
