@@ -32,3 +32,19 @@ def test_model_truncation_error(S, bits, bound):
         e64, _ = oracle.tuple_energies(oracle.Problem(d), 0, n, use_j=False)
         rel = np.max(np.abs(e - e64)) / np.max(np.abs(e64))
         assert rel <= bound, (No, Nv, rel)
+
+
+def test_newton_reciprocal_bound():
+    """The split kernel's energy denominators use 1/d = x0 + x0 (1 - d x0)
+    with x0 the correctly rounded FP32 reciprocal of FP32(d): emulated here
+    (numpy float32 division rounds to nearest like the FP32 reciprocal
+    instruction), the relative error stays below 2^-44 over the range of
+    orbital-energy gaps and beyond."""
+    rng = np.random.default_rng(7)
+    d = np.concatenate([np.exp(rng.uniform(np.log(1e-6), np.log(1e6), 200000)),
+                        -np.exp(rng.uniform(np.log(1e-3), np.log(1e3), 1000))])
+    x0 = (np.float32(1.0) / d.astype(np.float32)).astype(np.float64)
+    e = 1.0 - d * x0  # the kernel forms this with one FMA
+    x1 = x0 + x0 * e
+    rel = np.abs(x1 * d - 1.0)
+    assert np.max(rel) <= 2.0 ** -44, np.max(rel)
