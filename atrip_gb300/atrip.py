@@ -151,8 +151,8 @@ _ATTRIBUTES = {  # src/atrip/Atrip.hpp:113-131, with the reference defaults
     "ooo_threads": 0,
     "ooo_blocks": 0,
     # GPU attributes (no counterpart in the reference)
-    "form": "fp64",          # "fp64" | "split_bf16" | "auto"
-    "slices": 0,             # split form: BF16 slices per operand (0 = default 3)
+    "form": "fp64",          # "fp64" | "split_bf16" | "split_f16" | "auto"
+    "slices": 0,             # split forms: slices per operand (0 = 3 BF16 / 2 FP16)
     "device": 0,
     "checkpoint_chunks": 100,  # tuple chunks per run when checkpoints are written
 }

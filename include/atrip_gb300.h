@@ -68,7 +68,8 @@ enum atrip_form {
   ATRIP_FORM_FP64 = 0,       /* FP64 throughout                               */
   ATRIP_FORM_SPLIT_BF16 = 1, /* operands cut into BF16 slices, tensor cores,  */
                              /* FP32 accumulation, FP64 recombination         */
-  ATRIP_FORM_AUTO = 2,       /* the context's tuned choice                    */
+  ATRIP_FORM_AUTO = 2,       /* split-BF16 for real inputs (3 slices unless  */
+                             /* given), FP64 for complex                      */
   ATRIP_FORM_SPLIT_F16 = 3   /* 2 FP16 slices of 11-bit digits (22 bits per  */
                              /* operand, the MMAs of 2 BF16 slices); level 0  */
                              /* FP32-rounded; needs No <= 63 and              */
