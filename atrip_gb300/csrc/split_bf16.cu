@@ -948,8 +948,12 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 5-D BF16 tensor map: dims[0] fastest (K, padded), 128-byte swizzle.
-int make_map(CUtensorMap *m, const void *base, const uint64_t dims[5], const uint32_t box[5]) {
+// 5-D BF16 tensor map: dims[0] fastest (K, padded: the row pitch),
+// 128-byte swizzle.  kext (if nonzero) is the K extent the map declares:
+// the zero padding between kext and the pitch is then filled by TMA
+// instead of being read from memory.
+int make_map(CUtensorMap *m, const void *base, const uint64_t dims[5], const uint32_t box[5],
+             uint64_t kext = 0) {
   auto fn = encode_fn();
   if (!fn) {
     set_error("cuTensorMapEncodeTiled not available from the driver");
@@ -962,7 +966,8 @@ int make_map(CUtensorMap *m, const void *base, const uint64_t dims[5], const uin
     s *= dims[i + 1];
   }
   const uint32_t estr[5] = {1, 1, 1, 1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(base), dims, strides,
+  const uint64_t ext[5] = {kext ? kext : dims[0], dims[1], dims[2], dims[3], dims[4]};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(base), ext, strides,
                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
@@ -1075,25 +1080,25 @@ int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, int bi
   {
     const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt, 1, 1};
-    if ((rc = make_map(&p->maps.TaN, p->TaS, d, box))) return rc;
-    if ((rc = make_map(&p->maps.TaT, p->TaST, d, box))) return rc;
+    if ((rc = make_map(&p->maps.TaN, p->TaS, d, box, (uint64_t)Nv))) return rc;
+    if ((rc = make_map(&p->maps.TaT, p->TaST, d, box, (uint64_t)Nv))) return rc;
   }
   {
     const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt, 1, 1};
-    if ((rc = make_map(&p->maps.VhN, p->VhS, d, box))) return rc;
-    if ((rc = make_map(&p->maps.VhT, p->VhST, d, box))) return rc;
+    if ((rc = make_map(&p->maps.VhN, p->VhS, d, box, (uint64_t)No))) return rc;
+    if ((rc = make_map(&p->maps.VhT, p->VhST, d, box, (uint64_t)No))) return rc;
   }
   {
     const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)NP, 1, 1, 1};
-    if ((rc = make_map(&p->maps.Vp, p->VpS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.Vp, p->VpS, d, box, (uint64_t)Nv))) return rc;
   }
   {
     const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)NP, 1, 1, 1};
-    if ((rc = make_map(&p->maps.TpN, p->TpS, d, box))) return rc;
-    if ((rc = make_map(&p->maps.TpT, p->TpTS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.TpN, p->TpS, d, box, (uint64_t)No))) return rc;
+    if ((rc = make_map(&p->maps.TpT, p->TpTS, d, box, (uint64_t)No))) return rc;
   }
   // transposed variant: (p,q)-row boxes of jt2 row groups, r-column boxes
   // of all S slices (loaded from slice -sa, the rows below 0 read as zeros)
@@ -1101,37 +1106,37 @@ int prepare(SplitImpl *p, const DeviceTensors &dt, int No, int Nv, int S, int bi
   {
     const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt2, 1, 1};
-    if ((rc = make_map(&p->maps.TaN2, p->TaS, d, box))) return rc;
-    if ((rc = make_map(&p->maps.TaT2, p->TaST, d, box))) return rc;
+    if ((rc = make_map(&p->maps.TaN2, p->TaS, d, box, (uint64_t)Nv))) return rc;
+    if ((rc = make_map(&p->maps.TaT2, p->TaST, d, box, (uint64_t)Nv))) return rc;
   }
   {
     const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt2, 1, 1};
-    if ((rc = make_map(&p->maps.VhN2, p->VhS, d, box))) return rc;
-    if ((rc = make_map(&p->maps.VhT2, p->VhST, d, box))) return rc;
+    if ((rc = make_map(&p->maps.VhN2, p->VhS, d, box, (uint64_t)No))) return rc;
+    if ((rc = make_map(&p->maps.VhT2, p->VhST, d, box, (uint64_t)No))) return rc;
   }
   {
     const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)S};
-    if ((rc = make_map(&p->maps.Vp2, p->VpS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.Vp2, p->VpS, d, box, (uint64_t)Nv))) return rc;
   }
   {
     const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)S};
-    if ((rc = make_map(&p->maps.TpN2, p->TpS, d, box))) return rc;
-    if ((rc = make_map(&p->maps.TpT2, p->TpTS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.TpN2, p->TpS, d, box, (uint64_t)No))) return rc;
+    if ((rc = make_map(&p->maps.TpT2, p->TpTS, d, box, (uint64_t)No))) return rc;
   }
   // shared M stacks: 2S-1 slices from slice -(S-1)
   {
     const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)(2 * S - 1)};
-    if ((rc = make_map(&p->maps.Vp3, p->VpS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.Vp3, p->VpS, d, box, (uint64_t)Nv))) return rc;
   }
   {
     const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)(2 * S - 1)};
-    if ((rc = make_map(&p->maps.TpN3, p->TpS, d, box))) return rc;
-    if ((rc = make_map(&p->maps.TpT3, p->TpTS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.TpN3, p->TpS, d, box, (uint64_t)No))) return rc;
+    if ((rc = make_map(&p->maps.TpT3, p->TpTS, d, box, (uint64_t)No))) return rc;
   }
   p->maps.JhN = p->maps.VhN;
   p->maps.JhT = p->maps.VhT;
@@ -1182,30 +1187,30 @@ int prepare_j(SplitImpl *p, const DeviceTensors &dt, cudaStream_t st, int64_t *l
   {
     const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt, 1, 1};
-    if ((rc = make_map(&p->maps.JhN, p->JhS, d, box))) return rc;
-    if ((rc = make_map(&p->maps.JhT, p->JhST, d, box))) return rc;
+    if ((rc = make_map(&p->maps.JhN, p->JhS, d, box, (uint64_t)No))) return rc;
+    if ((rc = make_map(&p->maps.JhT, p->JhST, d, box, (uint64_t)No))) return rc;
   }
   {
     const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)NP, 1, 1, 1};
-    if ((rc = make_map(&p->maps.Jp, p->JpS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.Jp, p->JpS, d, box, (uint64_t)Nv))) return rc;
   }
   const int jt2 = 256 / No;
   {
     const uint64_t d[5] = {kHoleK, (uint64_t)No, (uint64_t)No, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, (uint32_t)jt2, 1, 1};
-    if ((rc = make_map(&p->maps.JhN2, p->JhS, d, box))) return rc;
-    if ((rc = make_map(&p->maps.JhT2, p->JhST, d, box))) return rc;
+    if ((rc = make_map(&p->maps.JhN2, p->JhS, d, box, (uint64_t)No))) return rc;
+    if ((rc = make_map(&p->maps.JhT2, p->JhST, d, box, (uint64_t)No))) return rc;
   }
   {
     const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)S};
-    if ((rc = make_map(&p->maps.Jp2, p->JpS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.Jp2, p->JpS, d, box, (uint64_t)Nv))) return rc;
   }
   {
     const uint64_t d[5] = {(uint64_t)Ep, (uint64_t)No, (uint64_t)Nv, (uint64_t)Nv, (uint64_t)S};
     const uint32_t box[5] = {kKChunk, (uint32_t)No, 1, 1, (uint32_t)(2 * S - 1)};
-    if ((rc = make_map(&p->maps.Jp3, p->JpS, d, box))) return rc;
+    if ((rc = make_map(&p->maps.Jp3, p->JpS, d, box, (uint64_t)Nv))) return rc;
   }
   p->has_j = true;
   return ATRIP_OK;
