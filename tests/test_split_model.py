@@ -48,3 +48,15 @@ def test_newton_reciprocal_bound():
     x1 = x0 + x0 * e
     rel = np.abs(x1 * d - 1.0)
     assert np.max(rel) <= 2.0 ** -44, np.max(rel)
+
+
+@pytest.mark.parametrize("S,bits,bound", [(3, 8, 1e-6), (2, 11, 5e-6)])
+def test_model_ct_truncation_error(S, bits, bound):
+    """(cT) energies of the digit model (T from the J intermediates) within
+    the same per-tuple bounds against the FP64 oracle."""
+    d = synth.make_inputs(8, 20, 1, with_j=True)
+    n = 60
+    _, ect = split_model.split_tuple_energies(d, S, 0, n, use_j=True, bits=bits)
+    e64, ect64 = oracle.tuple_energies(oracle.Problem(d), 0, n, use_j=True)
+    rel = np.max(np.abs(ect - ect64)) / np.max(np.abs(e64))
+    assert rel <= bound, rel
