@@ -267,10 +267,8 @@ struct KernelShape {
 // columns).  Stage: 16 KB M-side tile + 32 KB N-side tile.
 template <int S, bool MSHARE = false>
 struct KernelShapeT {
-  static constexpr int kNacc = 1;
   static constexpr int kBufCols = 256;
   static constexpr int kNbuf = 2;
-  static constexpr int kCols = 512;
   static constexpr int kAllocCols = 512;
   static constexpr int kBTile = 256 * 128;
   // MSHARE: the ring holds N-side tiles only; the M-side stacks live in two
