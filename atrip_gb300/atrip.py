@@ -1,5 +1,9 @@
 """Python mirror of atrip's public interface (src/atrip/Atrip.hpp:41-140).
 
+Under torch.distributed (one process per GPU, ``Atrip.init(group)``) the
+tuple list is split into contiguous shares and the energies merged at the
+end (``atrip_gb300.shard``).
+
 ``Atrip.init``, the ``Input`` builder with every ``with_*`` attribute and
 its default, ``Output(energy, ct_energy)`` and ``Atrip.run`` behave as in the
 reference, but the tuple loop runs on one GB300 through the C ABI
@@ -21,7 +25,7 @@ from typing import Callable, Optional
 
 import numpy as np
 
-from . import capi
+from . import capi, shard
 
 
 @dataclass
@@ -224,22 +228,120 @@ def _is_complex(t) -> bool:
 
 
 class Atrip:
-    """src/atrip/Atrip.hpp:41-63.  One process drives one GPU: rank 0 of 1."""
+    """src/atrip/Atrip.hpp:41-63.  One process drives one GPU; several
+    processes (torch.distributed ranks, one GPU each) split the tuple list
+    into contiguous shares and merge their compensated sums at the end."""
 
     rank = 0
     np = 1
+    group = None
     chrono: dict = {}
     Input = Input
     Output = Output
 
     @staticmethod
     def init(comm=None) -> None:
-        """src/atrip/Atrip.cxx:54-63; the communicator is accepted and unused."""
-        Atrip.rank, Atrip.np = 0, 1
+        """src/atrip/Atrip.cxx:54-63.  ``comm``: None (one process), or a
+        torch.distributed process group; with None and an initialised
+        default group, that group is used."""
+        Atrip.rank, Atrip.np, Atrip.group = 0, 1, None
+        try:
+            import torch.distributed as dist
+            if dist.is_available() and dist.is_initialized():
+                Atrip.group = comm
+                Atrip.rank = dist.get_rank(comm)
+                Atrip.np = dist.get_world_size(comm)
+        except ImportError:  # pragma: no cover
+            pass
         Atrip.chrono = {}
 
     @staticmethod
     def run(inp: Input) -> Output:
+        """src/atrip/Atrip.cxx:66-1133 on one GPU per process."""
+        if inp.ei is None or inp.ea is None:
+            raise ValueError("epsilon_i and epsilon_a are required")
+        No, Nv = _lens(inp.ei)[0], _lens(inp.ea)[0]
+        t_start = time.perf_counter()
+        # run<Complex> (src/atrip/Atrip.cxx:1136) when the inputs are complex
+        cplx = any(_is_complex(getattr(inp, attr)) for attr, _ in _TENSORS.values()
+                   if getattr(inp, attr) is not None)
+        device = inp.device
+        if Atrip.np > 1 and "LOCAL_RANK" in os.environ:
+            device = int(os.environ["LOCAL_RANK"])
+        with capi.Context(No, Nv, device, field="complex" if cplx else "real") as ctx:
+            for key, (attr, cname) in _TENSORS.items():
+                t = getattr(inp, attr)
+                if t is None:
+                    continue
+                ctx.upload(cname, _payload(t, cplx))
+            if inp.delete_Vppph:
+                inp.Vppph = None  # the caller's V_pphp is dropped as in src/atrip/Atrip.cxx:310
+            n = capi.n_tuples(Nv)
+            first, start_energy = 0, 0.0
+            if inp.read_checkpoint_if_exists and os.path.exists(inp.checkpoint_path):
+                c = read_checkpoint(inp.checkpoint_path)
+                first, start_energy = int(c.iteration), float(c.energy)
+            end = n if inp.max_iterations == 0 else min(n, inp.max_iterations + 1)
+            opts = dict(form=inp.form, slices=inp.slices, ijkabc=inp.ijkabc, use_j=True)
+            if Atrip.np > 1:
+                energy, ct = Atrip._run_shard(ctx, first, end, start_energy, opts, inp.ijkabc)
+                Atrip.chrono["run"] = time.perf_counter() - t_start
+                return Output(energy, ct)
+            # write condition of src/atrip/Atrip.cxx:588-591, 713:
+            # only a zero modulus writes (at every iteration in the reference;
+            # here at chunk boundaries of the device queue)
+            mod = (inp.checkpoint_at_every_iteration if inp.checkpoint_at_every_iteration != 0
+                   else int(n * inp.checkpoint_at_percentage / 100))
+            write = mod == 0
+            if not write:
+                r = ctx.run(first_iteration=first, max_iterations=inp.max_iterations,
+                            start_energy=start_energy, **opts)
+                energy, ct = r.energy, r.ct_energy
+                Atrip.chrono["iterations"] = r.device_ms / 1e3
+            else:
+                chunk = max(1, -(-(end - first) // max(1, int(inp.checkpoint_chunks))))
+                energy_phys, ct_acc = start_energy, 0.0
+                sign = 1.0 if inp.ijkabc else -1.0
+                pos = first
+                while pos < end:
+                    write_checkpoint(Checkpoint(No, Nv, 1, 1, energy_phys, pos,
+                                                inp.rank_round_robin), inp.checkpoint_path)
+                    stop = min(end, pos + chunk)
+                    r = ctx.run(first_iteration=pos, max_iterations=stop - 1,
+                                start_energy=energy_phys, **opts)
+                    energy_phys = r.energy if not inp.ijkabc else -r.energy
+                    ct_acc += sign * r.ct_energy
+                    pos = stop
+                    if _descriptor:
+                        _descriptor(IterationDescription(pos, n, time.perf_counter() - t_start))
+                energy = energy_phys if not inp.ijkabc else -energy_phys
+                ct = sign * ct_acc
+        Atrip.chrono["run"] = time.perf_counter() - t_start
+        return Output(energy, ct)
+
+    @staticmethod
+    def _run_shard(ctx, first, end, start_energy, opts, ijkabc):
+        """This rank's contiguous share of tuples first .. end-1, then the
+        merge of every rank's compensated sums (the role of atrip's
+        MPI_Reduce, src/atrip/Atrip.cxx:1094-1107).  Checkpoints are read
+        (resume point and energy) but not written across processes."""
+        t0, t1 = shard.tuple_range(first, end, Atrip.rank, Atrip.np)
+        local = (0.0, 0.0, 0.0, 0.0)
+        if t1 > t0:
+            if t1 - 1 == 0 and end > 1:
+                # max_iterations = 0 would mean "every tuple": run two and
+                # keep the first one's energies
+                ctx.run(first_iteration=0, max_iterations=1, **opts)
+                e, ect = ctx.tuple_energies(0, 1)
+                local = (float(e[0]), 0.0, float(ect[0]), 0.0)
+            else:
+                r = ctx.run(first_iteration=t0, max_iterations=t1 - 1, **opts)
+                Atrip.chrono["iterations"] = r.device_ms / 1e3
+                local = ctx.last_sums()
+        return shard.reduce_energies(local, ijkabc, start_energy, Atrip.group)
+
+
+def run(inp: Input) -> Output:
         """src/atrip/Atrip.cxx:66-1133 on one GPU."""
         if inp.ei is None or inp.ea is None:
             raise ValueError("epsilon_i and epsilon_a are required")

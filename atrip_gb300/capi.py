@@ -28,7 +28,8 @@ EXPORTED = [
     "atrip_gpu_destroy", "atrip_gpu_last_error", "atrip_gpu_version", "atrip_gpu_measure_peaks",
     "atrip_gpu_run_fp64_noalloc", "atrip_gpu_batch_create", "atrip_gpu_batch_run",
     "atrip_gpu_batch_destroy", "atrip_gpu_batch_plan", "atrip_gpu_set_tuning",
-    "atrip_gpu_get_tuning", "atrip_gpu_batch_set_tuning",
+    "atrip_gpu_get_tuning", "atrip_gpu_batch_set_tuning", "atrip_gpu_last_sums",
+    "atrip_gpu_device_count",
 ]
 
 
@@ -123,6 +124,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.atrip_gpu_set_tuning.argtypes = [P, ctypes.POINTER(Tuning)]
     lib.atrip_gpu_get_tuning.argtypes = [P, ctypes.POINTER(Tuning)]
     lib.atrip_gpu_batch_set_tuning.argtypes = [P, ctypes.POINTER(Tuning)]
+    lib.atrip_gpu_last_sums.argtypes = [P, ctypes.POINTER(ctypes.c_double)]
+    lib.atrip_gpu_device_count.argtypes = [ctypes.POINTER(ctypes.c_int32)]
     for name in EXPORTED:
         if name not in ("atrip_gpu_n_tuples", "atrip_gpu_last_error", "atrip_gpu_version"):
             getattr(lib, name).restype = ctypes.c_int
@@ -208,6 +211,13 @@ class Context:
         t = Tuning()
         check(self.lib.atrip_gpu_get_tuning(self.h, ctypes.byref(t)))
         return t.as_dict()
+
+    def last_sums(self):
+        """(sum, compensation) of the last run's per-tuple energies and of
+        its (cT) energies: (s_e, c_e, s_ct, c_ct), no sign applied."""
+        out = (ctypes.c_double * 4)()
+        check(self.lib.atrip_gpu_last_sums(self.h, out))
+        return tuple(out)
 
     def tuple_energies(self, t0: int, n: int):
         import numpy as np

@@ -373,7 +373,7 @@ int atrip_gpu_create(const atrip_dims *dims, atrip_gpu_context **out) {
   CREATE_TRY(cudaMalloc(&c->d_ect, sizeof(double) * std::max<int64_t>(c->n_tuples, 1)));
   CREATE_TRY(cudaMalloc(&c->d_queue, sizeof(unsigned long long) * 4));
   CREATE_TRY(cudaMalloc(&c->d_partials, sizeof(double) * 4 * kSumBlocks));
-  CREATE_TRY(cudaMalloc(&c->d_sum, sizeof(double) * 4));
+  CREATE_TRY(cudaMalloc(&c->d_sum, sizeof(double) * 8));
 #undef CREATE_TRY
   *out = c;
   return ATRIP_OK;
@@ -501,15 +501,16 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
     launches += 2;
   }
   ATRIP_CUDA_TRY(cudaEventRecord(c->ev1, st));
-  double sums[2] = {0.0, 0.0};
+  double sums[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   if (n > 0)
-    ATRIP_CUDA_TRY(cudaMemcpyAsync(sums, c->d_sum, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
+    ATRIP_CUDA_TRY(cudaMemcpyAsync(sums, c->d_sum, sizeof(double) * 6, cudaMemcpyDeviceToHost, st));
   ATRIP_CUDA_TRY(cudaStreamSynchronize(st));
   ATRIP_CUDA_TRY(cudaGetLastError());
   float ms = 0.f;
   ATRIP_CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->e_lo = t_begin;
   c->e_hi = t_end;
+  for (int k = 0; k < 4; ++k) c->last_sums[k] = sums[2 + k];
   // local energy starts at -checkpoint energy (src/atrip/Atrip.cxx:612-616);
   // final sign flip unless ijkabc (src/atrip/Atrip.cxx:1108-1111)
   const double sign = opts->ijkabc ? 1.0 : -1.0;
@@ -560,6 +561,25 @@ int atrip_gpu_tuple_energies(atrip_gpu_context *c, int64_t t0, int64_t n, double
   if (e) ATRIP_CUDA_TRY(cudaMemcpy(e, c->d_e + t0, sizeof(double) * n, cudaMemcpyDeviceToHost));
   if (ect)
     ATRIP_CUDA_TRY(cudaMemcpy(ect, c->d_ect + t0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return ATRIP_OK;
+}
+
+int atrip_gpu_device_count(int32_t *count) {
+  clear_error();
+  if (!count) return fail(ATRIP_ERR_ARGUMENT, "null argument");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    n = 0;
+  }
+  *count = n;
+  return ATRIP_OK;
+}
+
+int atrip_gpu_last_sums(const atrip_gpu_context *c, double *sums) {
+  clear_error();
+  if (!c || !sums) return fail(ATRIP_ERR_ARGUMENT, "null argument");
+  for (int k = 0; k < 4; ++k) sums[k] = c->last_sums[k];
   return ATRIP_OK;
 }
 

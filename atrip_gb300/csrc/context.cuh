@@ -22,6 +22,7 @@ struct atrip_gpu_context {
   uint32_t *d_triples = nullptr;
   double *d_e = nullptr, *d_ect = nullptr;
   int64_t e_lo = 0, e_hi = 0;  // tuple range holding energies of the last run
+  double last_sums[4] = {};    // (sum, compensation) of e and ect over that range
   double *d_workspace = nullptr;
   size_t workspace_doubles = 0;
   unsigned long long *d_queue = nullptr;

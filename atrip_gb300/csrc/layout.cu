@@ -93,6 +93,11 @@ __global__ void energy_sum_stage2(const double *__restrict__ partials, int nb,
     }
     out[0] = s0 + c0;
     out[1] = s1 + c1;
+    // the compensated pairs themselves, for exact merging across processes
+    out[2] = s0;
+    out[3] = c0;
+    out[4] = s1;
+    out[5] = c1;
   }
 }
 

@@ -24,7 +24,6 @@
 // the get_energy_{distinct,same} terms of src/atrip/Equations.cxx:101-238).
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "atrip_gb300.h"
@@ -338,29 +337,21 @@ int launch(const Args &a, int device, cudaStream_t st) {
   return ATRIP_OK;
 }
 
-// Device address of g_scratch, looked up once per device with that device
-// current.
-unsigned char *scratch_address(int device, int *status) {
-  static std::mutex mu;
-  static unsigned char *addr[64] = {};
-  std::lock_guard<std::mutex> lock(mu);
-  if (device < 0 || device >= 64) {
-    set_error("device ordinal out of range");
-    *status = ATRIP_ERR_ARGUMENT;
+// Device address of g_scratch on the current device.  Looked up on every
+// call (cudaGetSymbolAddress is a cheap table lookup once the module is
+// loaded): an address cached across calls would go stale after a
+// cudaDeviceReset or a re-created primary context, which loads the module
+// again elsewhere.
+unsigned char *scratch_address(int *status) {
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaGetSymbolAddress(g_scratch): ") + cudaGetErrorString(e));
+    *status = ATRIP_ERR_CUDA;
     return nullptr;
   }
-  if (!addr[device]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess) {
-      set_error(std::string("cudaGetSymbolAddress(g_scratch): ") + cudaGetErrorString(e));
-      *status = ATRIP_ERR_CUDA;
-      return nullptr;
-    }
-    addr[device] = static_cast<unsigned char *>(p);
-  }
   *status = ATRIP_OK;
-  return addr[device];
+  return static_cast<unsigned char *>(p);
 }
 
 }  // namespace noalloc
@@ -399,7 +390,7 @@ extern "C" int atrip_gpu_run_fp64_noalloc(int32_t no, int32_t nv, const atrip_de
   int device = 0;
   ATRIP_CUDA_TRY(cudaGetDevice(&device));
   int status = ATRIP_OK;
-  unsigned char *scratch = noalloc::scratch_address(device, &status);
+  unsigned char *scratch = noalloc::scratch_address(&status);
   if (!scratch) return status;
   const int64_t n_all = atrip_gpu_n_tuples(nv);
   int64_t t_end = n_all;

@@ -11,7 +11,7 @@
 // CTF::Tensor<F>{lens, read_all}).
 //
 // Differences a caller can see:
-//  * one process drives one GPU; rank() is 0 and np is 1;
+//  * one process drives one GPU; Atrip::rank is 0 and Atrip::np is 1;
 //  * TuplesDistribution is accepted, and both values map to the on-device
 //    work queue over atrip's lexicographic tuple list;
 //  * checkpoints keep atrip's YAML format and resume semantics; when atrip
@@ -24,7 +24,9 @@
 #ifndef ATRIP_GB300_ATRIP_HPP_
 #define ATRIP_GB300_ATRIP_HPP_
 
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <complex>
 #include <cstdint>
 #include <cstdio>
@@ -40,6 +42,9 @@
 #include <ctf.hpp>
 
 #include <atrip_gb300.h>
+#include <atrip/Chrono.hpp>
+#include <atrip/Complex.hpp>
+#include <atrip/Debug.hpp>
 
 #define ATRIP_GB300_ADD_ATTRIBUTE(_type, _name, _default)                     \
   _type _name = _default;                                                      \
@@ -49,24 +54,6 @@
   }
 
 namespace atrip {
-
-using Complex = std::complex<double>;
-
-// src/atrip/Debug.hpp:96-109
-struct IterationDescription;
-using IterationDescriptor = std::function<void(IterationDescription const &)>;
-struct IterationDescription {
-  static IterationDescriptor &descriptor() {
-    static IterationDescriptor d;
-    return d;
-  }
-  size_t current_iteration;
-  size_t total_iterations;
-  double current_elapsed_time;
-};
-inline void register_iteration_descriptor(IterationDescriptor d) {
-  IterationDescription::descriptor() = d;
-}
 
 // src/atrip/Checkpoint.hpp:27-79
 struct Checkpoint {
@@ -116,23 +103,24 @@ inline Checkpoint read_checkpoint(std::string const &filepath) {
 }
 
 struct Atrip {
-  static size_t &rank_ref() {
-    static size_t r = 0;
-    return r;
-  }
-  static size_t &np_ref() {
-    static size_t n = 1;
-    return n;
-  }
-  static std::map<std::string, double> &chrono() {
-    static std::map<std::string, double> m;
-    return m;
-  }
+  // src/atrip/Atrip.hpp:43-47: process-wide state read by drivers
+  // (atrip's bench prints the energy where rank == 0)
+  inline static size_t rank = 0;
+  inline static size_t np = 1;
+  inline static Timings chrono;
+  inline static MPI_Comm communicator = MPI_COMM_WORLD;
 
-  // src/atrip/Atrip.cxx:54-63: one process, one GPU.
-  static void init(MPI_Comm) {
-    rank_ref() = 0;
-    np_ref() = 1;
+  // src/atrip/Atrip.cxx:54-63.  One process drives one GPU; with several
+  // ranks each runs a contiguous share of the tuple list on its own GPU
+  // (device attribute + rank, modulo the GPUs it sees) and the energies are
+  // merged at the end.
+  static void init(MPI_Comm c) {
+    int r = 0, n = 1;
+    MPI_Comm_rank(c, &r);
+    MPI_Comm_size(c, &n);
+    communicator = c;
+    rank = (size_t)r;
+    np = (size_t)n;
   }
 
   template <typename F = double>
@@ -206,6 +194,60 @@ struct ContextGuard {
   ~ContextGuard() { atrip_gpu_destroy(c); }
 };
 
+inline void neumaier(double &s, double &c, double x) {
+  const double t = s + x;
+  c += std::fabs(s) >= std::fabs(x) ? (s - t) + x : (x - t) + s;
+  s = t;
+}
+
+// Rank `Atrip::rank`'s contiguous share of tuples first .. end-1 (sizes
+// differ by at most one), then every rank's compensated sums gathered and
+// merged in rank order -- the role of atrip's final MPI_Reduce
+// (src/atrip/Atrip.cxx:1094-1107); every rank returns the total.
+// Checkpoints are read but not written across ranks.
+inline Atrip::Output run_share(atrip_gpu_context *ctx, atrip_run_options o, size_t first,
+                               size_t end, double start_energy, bool ijkabc);
+
+}  // namespace detail
+
+inline Atrip::Output detail::run_share(atrip_gpu_context *ctx, atrip_run_options o, size_t first,
+                                       size_t end, double start_energy, bool ijkabc) {
+  const size_t n = end > first ? end - first : 0, P = Atrip::np, R = Atrip::rank;
+  const size_t base = n / P, extra = n % P;
+  const size_t t0 = first + R * base + std::min(R, extra);
+  const size_t t1 = t0 + base + (R < extra ? 1 : 0);
+  double local[4] = {0.0, 0.0, 0.0, 0.0};
+  if (t1 > t0) {
+    atrip_result r{};
+    if (t1 == 1 && end > 1) {
+      // max_iterations = 0 would mean "every tuple": run two, keep the first
+      o.first_iteration = 0;
+      o.max_iterations = 1;
+      check(atrip_gpu_run(ctx, &o, &r));
+      check(atrip_gpu_tuple_energies(ctx, 0, 1, &local[0], &local[2]));
+    } else {
+      o.first_iteration = (int64_t)t0;
+      o.max_iterations = (int64_t)t1 - 1;
+      check(atrip_gpu_run(ctx, &o, &r));
+      check(atrip_gpu_last_sums(ctx, local));
+    }
+  }
+  std::vector<double> all(4 * P);
+  MPI_Allgather(local, 4, MPI_DOUBLE, all.data(), 4, MPI_DOUBLE, Atrip::communicator);
+  double se = 0, ce = 0, sc = 0, cc = 0;
+  for (size_t p = 0; p < P; ++p) {
+    neumaier(se, ce, all[4 * p + 0]);
+    neumaier(se, ce, all[4 * p + 1]);
+    neumaier(sc, cc, all[4 * p + 2]);
+    neumaier(sc, cc, all[4 * p + 3]);
+  }
+  neumaier(se, ce, -start_energy);  // src/atrip/Atrip.cxx:612-616
+  const double sign = ijkabc ? 1.0 : -1.0;
+  return {sign * (se + ce), sign * (sc + cc)};
+}
+
+namespace detail {
+
 }  // namespace detail
 
 // src/atrip/Atrip.cxx:66-1133 on one GPU, for F = double or Complex
@@ -218,7 +260,13 @@ inline Atrip::Output Atrip::run_field(Atrip::Input<F> const &in, int32_t field) 
   if (!in.ei || !in.ea || !in.Tph || !in.Tpphh || !in.Vpphh || !in.Vhhhp || !in.Vppph)
     throw std::string("atrip_gb300: Atrip::run needs ei, ea, Tai, Tabij, Vabij, Vijka, Vabci");
   const size_t No = in.ei->lens[0], Nv = in.ea->lens[0];
-  atrip_dims dims{(int32_t)No, (int32_t)Nv, in.device, field};
+  int32_t device = in.device;
+  if (np > 1) {
+    int32_t count = 0;
+    if (atrip_gpu_device_count(&count) == ATRIP_OK && count > 0)
+      device = (int32_t)((in.device + rank) % (size_t)count);
+  }
+  atrip_dims dims{(int32_t)No, (int32_t)Nv, device, field};
   detail::ContextGuard g;
   detail::check(atrip_gpu_create(&dims, &g.c));
   struct Slot {
@@ -266,6 +314,11 @@ inline Atrip::Output Atrip::run_field(Atrip::Input<F> const &in, int32_t field) 
   o.use_j = 1;
   Output result{0.0, 0.0};
   atrip_result r{};
+  if (np > 1) {
+    result = detail::run_share(g.c, o, first, end, start_energy, in.ijkabc);
+    chrono["run"].add(std::chrono::duration<double>(clock::now() - t_start).count());
+    return result;
+  }
   if (mod != 0) {
     o.first_iteration = (int64_t)first;
     o.max_iterations = (int64_t)in.max_iterations;
@@ -294,8 +347,8 @@ inline Atrip::Output Atrip::run_field(Atrip::Input<F> const &in, int32_t field) 
     result = {in.ijkabc ? -ck_energy : ck_energy, sign * ct_local};
     if (end <= first) result.energy = in.ijkabc ? -start_energy : start_energy;
   }
-  chrono()["iterations"] = r.device_ms / 1e3;
-  chrono()["run"] = std::chrono::duration<double>(clock::now() - t_start).count();
+  chrono["iterations"].add(r.device_ms / 1e3);
+  chrono["run"].add(std::chrono::duration<double>(clock::now() - t_start).count());
   return result;
 }
 

@@ -119,6 +119,11 @@ typedef struct {
   int64_t kernel_launches; /* kernels this library launched in the run        */
 } atrip_result;
 
+/* Number of CUDA devices this process sees (0 without a driver or GPU).
+ * Ranks of a multi-process run pick theirs from it (one GPU per rank, the
+ * device assignment atrip's ranks get from their node-local rank). */
+int atrip_gpu_device_count(int32_t *count);
+
 /* Create a context on dims->device.  Replaces the per-rank device setup of
  * Atrip::run (src/atrip/Atrip.cxx:78-171) and the tuple list
  * (src/atrip/Tuples.cxx:89-134, built once on the host, kept on device). */
@@ -179,6 +184,16 @@ typedef struct {
 /* Set / read the context's launch parameters (kept until changed). */
 int atrip_gpu_set_tuning(atrip_gpu_context *ctx, const atrip_tuning *tuning);
 int atrip_gpu_get_tuning(const atrip_gpu_context *ctx, atrip_tuning *tuning);
+
+/* The compensated sums behind the last run's result: sums[0] + sums[1] is
+ * the sum of its per-tuple energies (sums[1] the Neumaier compensation of
+ * sums[0]), sums[2] + sums[3] likewise for the (cT) energies; no sign and
+ * no checkpoint energy applied.  Processes that each run one contiguous
+ * share of the tuple list merge these pairs into the total exactly as
+ * atrip's final MPI_Reduce of the local energies does
+ * (src/atrip/Atrip.cxx:1094-1107), without the rounding of one double per
+ * process.                                                                 */
+int atrip_gpu_last_sums(const atrip_gpu_context *ctx, double *sums);
 
 /* Per-tuple energies of the last run, tuple-list positions t0 .. t0+n-1
  * (the sign atrip accumulates before its final negation). ect may be NULL. */
@@ -249,10 +264,16 @@ int atrip_gpu_batch_set_tuning(atrip_gpu_batch *batch, const atrip_tuning *tunin
  * loads the library holds that array until the process exits.  All calls
  * share it: each call clears what must start at zero, and calls whose
  * kernels overlap on the GPU (other streams, other host threads) race on it,
- * so serialise them.  The first call on a device looks the array's device
- * address up once (cudaGetSymbolAddress, with that device current); make
- * that first call before any stream capture.  Limits: 1 <= No <= 64 (2 No^3
- * doubles of W per CTA must fit in the array), 1 <= Nv <= 1023.
+ * so serialise them.  Every call looks the array's device address up on
+ * the current device (cudaGetSymbolAddress); the first call on a device
+ * also loads the library's device code there, so make that first call
+ * before any stream capture.  Limits: 1 <= No <= 64 (2 No^3 doubles of W
+ * per CTA must fit in the array; at large No this also caps the number of
+ * CTAs, e.g. 7 at No = 64), 1 <= Nv <= 1023.
+ *
+ * No checkpoint resume: unlike atrip_run_options there is no start_energy.
+ * A caller resuming from a checkpoint passes first_iteration = the saved
+ * Iteration and adds the saved energy to energies[0] itself.
  *
  * Tuples first_iteration .. max_iterations (inclusive; 0 = all) are run on
  * the current device, in `stream` (NULL = default stream); the call returns

@@ -42,10 +42,13 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_reference(reference: str = "/root/reference") -> bool:
+def build_reference(reference: str | None = None) -> bool:
     """Compile the reference's own sources with the shims into ``_ref/``.
-    Returns False when the reference tree is not present."""
-    if not os.path.isdir(os.path.join(reference, "src", "atrip")):
+    ``reference`` (default: the ``ATRIP_REFERENCE`` environment variable)
+    is the root of an atrip source tree.  Returns False when it is not
+    given or not present."""
+    reference = reference or os.environ.get("ATRIP_REFERENCE", "")
+    if not reference or not os.path.isdir(os.path.join(reference, "src", "atrip")):
         return False
     subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REFERENCE={reference}"])
     return True

@@ -1,7 +1,10 @@
 /* Dense, single-process stand-in for the subset of Cyclops (CTF) that the
  * atrip reference calls: World, Tensor<F>{order, lens, data, read_all,
  * slice} and the NS symmetry tag (src/atrip/SliceUnion.cxx:308-317,
- * src/atrip/Unions.hpp:21-75, src/atrip/Atrip.cxx:72-73,179-181).
+ * src/atrip/Unions.hpp:21-75, src/atrip/Atrip.cxx:72-73,179-181); and what
+ * atrip's own driver (bench/main.cxx) calls on top: World(argc, argv) and
+ * its np, fill_random, read_dense_from_file, norm2, index-labelled
+ * assignment (T["ijab"] = S["abij"]) and Transform<A, B>(f)(S["i"], T["i"]).
  *
  * Test infrastructure only.  Storage is column-major (first index fastest),
  * which is the element order CTF's read_all returns for a dense tensor and
@@ -19,6 +22,10 @@
 #include <iostream>
 #include <iomanip>
 #include <sstream>
+#include <fstream>
+#include <functional>
+#include <random>
+#include <complex>
 #include <mpi.h>
 
 using namespace std; // the reference relies on a transitive `using` (src/atrip/Tuples.hpp:68)
@@ -33,7 +40,57 @@ namespace CTF {
 class World {
 public:
   explicit World(MPI_Comm c = MPI_COMM_WORLD) : comm(c) {}
+  World(int, char **) : comm(MPI_COMM_WORLD) {}
   MPI_Comm comm;
+  int np = 1;
+};
+
+template <typename F> class Tensor;
+
+/* A tensor with one index label per mode ("abij"): the operand of labelled
+ * assignments and transforms.  Modes with equal labels are matched. */
+template <typename F>
+struct Idx_Tensor {
+  Tensor<F> *t;
+  std::string idx;
+  /* this[labels] = other[labels]: a permutation of the modes */
+  Idx_Tensor &operator=(const Idx_Tensor &o) {
+    Tensor<F>::assign_permuted(*t, idx, *o.t, o.idx);
+    return *this;
+  }
+};
+
+/* Transform<A, B>(f)(S["..."], T["..."]) calls f(s, t) for every pair of
+ * elements of S and T at matching labels; f updates t in place. */
+template <typename A, typename B = A>
+class Transform {
+public:
+  explicit Transform(std::function<void(A, B &)> f) : f_(f) {}
+  void operator()(const Idx_Tensor<A> &s, const Idx_Tensor<B> &t) const {
+    Tensor<B> &T = *t.t;
+    const Tensor<A> &S = *s.t;
+    std::vector<int> perm = label_map(t.idx, s.idx);
+    std::vector<int> idx(T.order, 0);
+    for (std::int64_t n = 0; n < T.size; ++n) {
+      std::int64_t lin = 0, stride = 1;
+      for (int d = 0; d < S.order; ++d) { lin += idx[perm[d]] * stride; stride *= S.lens[d]; }
+      f_(S.data[lin], T.data[n]);
+      for (int d = 0; d < T.order; ++d) { if (++idx[d] < T.lens[d]) break; idx[d] = 0; }
+    }
+  }
+  /* for each mode of `src`, the mode of `dst` with the same label */
+  static std::vector<int> label_map(const std::string &dst, const std::string &src) {
+    std::vector<int> m(src.size());
+    for (std::size_t d = 0; d < src.size(); ++d) {
+      const std::size_t p = dst.find(src[d]);
+      if (p == std::string::npos) throw std::string("ctf shim: unmatched index label");
+      m[d] = (int)p;
+    }
+    return m;
+  }
+
+private:
+  std::function<void(A, B &)> f_;
 };
 
 template <typename F = double>
@@ -51,6 +108,31 @@ public:
   ~Tensor() { delete[] lens; delete[] data; }
 
   void read_all(F *out) const { std::memcpy(out, data, sizeof(F) * size); }
+
+  Idx_Tensor<F> operator[](const char *idx) { return Idx_Tensor<F>{this, idx}; }
+
+  /* uniform random values in [a, b) (a fixed-seed stream: reproducible) */
+  void fill_random(F a, F b) {
+    std::mt19937_64 gen(0x5eed + (std::uint64_t)size);
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    for (std::int64_t n = 0; n < size; ++n) data[n] = a + (b - a) * F(u(gen));
+  }
+  /* dense column-major binary file of `size` elements */
+  void read_dense_from_file(const char *path) {
+    std::ifstream in(path, std::ios::binary);
+    if (!in.read(reinterpret_cast<char *>(data), sizeof(F) * size))
+      throw std::string("ctf shim: cannot read ") + path;
+  }
+  double norm2() const {
+    double s = 0.0;
+    for (std::int64_t n = 0; n < size; ++n) s += std::norm(data[n]);
+    return std::sqrt(s);
+  }
+  static void assign_permuted(Tensor &dst, const std::string &di, const Tensor &src,
+                              const std::string &si) {
+    Transform<F, F>([](F s, F &d) { d = s; })(Idx_Tensor<F>{const_cast<Tensor *>(&src), si},
+                                               Idx_Tensor<F>{&dst, di});
+  }
 
   /* this[offsets:ends] = beta * this[offsets:ends] + alpha * A[offsets_A:ends_A].
    * Both blocks are walked in column-major order; the reference only ever

@@ -61,6 +61,8 @@ inline int oracle_mpi_new_type(std::size_t extent) {
   std::abort();
 }
 
+inline int MPI_Init(int *, char ***) { return 0; }
+inline int MPI_Finalize() { return 0; }
 inline int MPI_Comm_rank(MPI_Comm, int *r) { *r = 0; return 0; }
 inline int MPI_Comm_size(MPI_Comm, int *s) { *s = 1; return 0; }
 inline int MPI_Comm_split(MPI_Comm c, int, int, MPI_Comm *out) { *out = c; return 0; }

@@ -19,7 +19,8 @@ DGEMM route is recorded and the naive variant's totals are kept beside it
 for the record.  The inputs are NOT stored: tests regenerate them from
 (No, Nv, seed, with_j, field, eps_imag).
 
-Usage (needs the reference tree; not part of the test run):
+Usage (needs the reference tree, given as the first argument or in the
+ATRIP_REFERENCE environment variable; not part of the test run):
     python tests/golden/make_golden.py [/path/to/reference] [name-prefix]
 """
 from __future__ import annotations
@@ -78,7 +79,7 @@ def dump(bin_dir: str, t: int):
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ATRIP_REFERENCE", "")
     prefix = sys.argv[2] if len(sys.argv) > 2 else ""
     if not oracle.build_reference(ref):
         raise SystemExit("reference tree not found: " + ref)

@@ -32,7 +32,7 @@ def _device_columns(d):
     return out
 
 
-def _noalloc(lib, No, Nv, dev, first, maxit, use_j):
+def _noalloc(lib, No, Nv, dev, first, maxit, use_j, ijkabc=0, drop_j=False):
     import torch
     n_all = capi.n_tuples(Nv)
     end = n_all if maxit == 0 else min(n_all, maxit + 1)
@@ -40,9 +40,10 @@ def _noalloc(lib, No, Nv, dev, first, maxit, use_j):
     e = torch.full((max(n, 1),), float("nan"), dtype=torch.float64, device="cuda:0")
     ect = torch.full((max(n, 1),), float("nan"), dtype=torch.float64, device="cuda:0")
     energies = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda:0")
-    ptrs = capi.DeviceInputs(*[dev[k].data_ptr() for k in NAMES])
+    ptrs = capi.DeviceInputs(*[None if drop_j and k in ("Jijka", "Jabci") else dev[k].data_ptr()
+                               for k in NAMES])
     torch.cuda.synchronize()
-    capi.check(lib.atrip_gpu_run_fp64_noalloc(No, Nv, ctypes.byref(ptrs), first, maxit, 0,
+    capi.check(lib.atrip_gpu_run_fp64_noalloc(No, Nv, ctypes.byref(ptrs), first, maxit, ijkabc,
                                               int(use_j), e.data_ptr(), ect.data_ptr(),
                                               energies.data_ptr(), None))
     torch.cuda.synchronize()
@@ -69,6 +70,52 @@ def test_noalloc_matches_regular_entry_point_twice():
             assert np.max(np.abs(ect - ref_ect)) <= REL * scale
             assert abs(energies[0] - ref.energy) <= REL * abs(ref.energy)
             assert abs(energies[1] - ref.ct_energy) <= REL * abs(ref.energy)
+
+
+def _compare(ctx, lib, No, Nv, dev, first, maxit, ijkabc=False, drop_j=False):
+    ref = ctx.run(form="fp64", first_iteration=first, max_iterations=maxit, ijkabc=ijkabc,
+                  use_j=not drop_j)
+    ref_e, ref_ect = ctx.tuple_energies(first, ref.tuples_done)
+    e, ect, energies = _noalloc(lib, No, Nv, dev, first, maxit, True, int(ijkabc), drop_j)
+    assert len(e) == ref.tuples_done
+    scale = np.max(np.abs(ref_e))
+    assert np.max(np.abs(e - ref_e)) <= REL * scale
+    assert np.max(np.abs(ect - ref_ect)) <= REL * scale
+    assert abs(energies[0] - ref.energy) <= REL * abs(ref.energy)
+    assert abs(energies[1] - ref.ct_energy) <= REL * abs(ref.energy)
+    return energies
+
+
+def test_noalloc_ijkabc_and_without_j():
+    """ijkabc (negated T1, no final negation) and NULL J pointers (then
+    ct_energy == energy), each against the regular entry point."""
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    No, Nv = 9, 13
+    d = synth.make_inputs(No, Nv, 22, with_j=True)
+    dev = _device_columns(d)
+    lib = capi.load()
+    with capi.Context(No, Nv, 0) as ctx:
+        for n in NAMES:
+            ctx.upload(n, d[n])
+        _compare(ctx, lib, No, Nv, dev, 0, 0, ijkabc=True)
+        energies = _compare(ctx, lib, No, Nv, dev, 3, 200, drop_j=True)
+        assert energies[1] == energies[0]
+
+
+def test_noalloc_large_no_grid_capped_by_scratch():
+    """At No=56 the 32 MiB array holds W for only 11 CTAs (2 No^3 doubles
+    each): fewer CTAs than the occupancy grid, every tuple still run."""
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    No, Nv = 56, 8
+    d = synth.make_inputs(No, Nv, 23, with_j=True)
+    dev = _device_columns(d)
+    lib = capi.load()
+    with capi.Context(No, Nv, 0) as ctx:
+        for n in NAMES:
+            ctx.upload(n, d[n])
+        _compare(ctx, lib, No, Nv, dev, 0, 60)
 
 
 def test_noalloc_rejects_out_of_range_sizes():
