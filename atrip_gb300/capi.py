@@ -67,7 +67,9 @@ class Tuning(ctypes.Structure):
                 ("tuples_per_claim", ctypes.c_int32), ("split_stages", ctypes.c_int32),
                 ("split_ctas", ctypes.c_int32), ("fp64_min_blocks", ctypes.c_int32),
                 ("split_w_global", ctypes.c_int32), ("tuple_block", ctypes.c_int32),
-                ("split_variant", ctypes.c_int32), ("split_prefetch", ctypes.c_int32)]
+                ("split_variant", ctypes.c_int32), ("split_prefetch", ctypes.c_int32),
+                ("split_wait_kcycles", ctypes.c_int32),
+                ("split_test_unpublished", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

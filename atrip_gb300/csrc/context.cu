@@ -487,6 +487,8 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
       c->split.w_global = c->tune.split_w_global != 0;
       c->split.variant = c->tune.split_variant;
       c->split.prefetch = c->tune.split_prefetch != 0;
+      c->split.wait_cycles = (long long)c->tune.split_wait_kcycles * 1000;
+      c->split.unpublished = c->tune.split_test_unpublished != 0;
       c->split.f16 = form == ATRIP_FORM_SPLIT_F16;
       const int ctas = c->tune.split_ctas > 0 ? std::min(c->sm_count, (int)c->tune.split_ctas)
                                               : c->sm_count;
@@ -541,6 +543,9 @@ int atrip_gpu_set_tuning(atrip_gpu_context *c, const atrip_tuning *t) {
   if (t->tuples_per_claim > 64) return fail(ATRIP_ERR_ARGUMENT, "tuples_per_claim must be <= 64");
   if (t->fp64_min_blocks != 0 && t->fp64_min_blocks != 2)
     return fail(ATRIP_ERR_ARGUMENT, "fp64_min_blocks must be 0 or 2");
+  if (t->split_wait_kcycles < 0) return fail(ATRIP_ERR_ARGUMENT, "negative wait limit");
+  if (t->split_test_unpublished != 0 && t->split_test_unpublished != 1)
+    return fail(ATRIP_ERR_ARGUMENT, "split_test_unpublished must be 0 or 1");
   c->tune = *t;
   return ATRIP_OK;
 }

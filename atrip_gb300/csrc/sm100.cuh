@@ -45,16 +45,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 // Wait for the phase with the given parity to complete.  Returns false (and
-// sets *status to code if it was 0) when the wait exceeds kWaitCycles or
-// another thread already reported a failure.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code) {
+// sets *status to code if it was 0) when the wait exceeds `limit` SM cycles
+// (default kWaitCycles) or another thread already reported a failure.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code,
+                                          long long limit = kWaitCycles) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 255u) == 0) {
       if (*reinterpret_cast<volatile int *>(status) != 0) return false;
-      if (clock64() - t0 > kWaitCycles) {
+      if (clock64() - t0 > limit) {
         atomicCAS(status, 0, code);
         return false;
       }

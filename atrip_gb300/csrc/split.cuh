@@ -19,6 +19,8 @@ struct SplitState {
   int variant = 0;          // 2: transposed kernel (stacked slices as M) where eligible
   bool prefetch = false;    // L2 prefetch of the next part's slab tiles
   bool f16 = false;         // FP16 digit slices (radix 2^11) instead of BF16 (2^8)
+  long long wait_cycles = 0;  // bounded-wait limit in SM cycles (0 = built-in ~2 s)
+  bool unpublished = false;   // test: the producer publishes no tuple
 };
 
 void split_invalidate(SplitState &s);

@@ -88,6 +88,8 @@ struct SplitArgs {
   int No, Nv, jt, ntiles, kch;  // j per M-tile, M-tiles per group, K chunks of Nv
   int jt2, ntiles2, nmma;       // transposed variant: q per N-tile, N-tiles, MMA N
   int prefetch;                 // 1: L2 prefetch of the next part's (p,q)-row tiles
+  int unpublished;              // test: the producer publishes no tuple (waits run out)
+  long long wait_cycles;        // limit of every bounded wait, SM cycles
   int mslot_bytes;              // MSHARE: bytes of one shared M-tile slot
   int nstages;                 // operand ring depth
   const double *epsi, *epsa, *tai, *Vhh;
@@ -394,13 +396,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (warp == 0) {
     // ------------------------------------------------------ TMA producer
-    if (lane == 0) {
+    if (lane == 0 && !g.unpublished) {
       uint32_t unit_count = 0, mcount = 0;
       bool alive = true;
       for (uint32_t k = 0;; ++k) {
         const int ts = k % kTupleSlots;
         const uint32_t tuse = k / kTupleSlots;
-        if (tuse > 0 && !mbar_wait(&tempty[ts], (tuse - 1) & 1, g.status, kErrTimeoutEmpty))
+        if (tuse > 0 && !mbar_wait(&tempty[ts], (tuse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles))
           alive = false;
         const unsigned long long q = alive ? atomicAdd(g.queue, 1ull) : ~0ull;
         const bool stop = !alive || q >= (unsigned long long)(g.t_end - g.t_begin) ||
@@ -448,7 +450,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                       const int ms = mcount % kMSlots;
                       const uint32_t muse = mcount / kMSlots;
                       if (muse > 0 &&
-                          !mbar_wait(&mempty[ms], (muse - 1) & 1, g.status, kErrTimeoutEmpty)) {
+                          !mbar_wait(&mempty[ms], (muse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles)) {
                         alive = false;
                         break;
                       }
@@ -460,7 +462,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                   }
                   const int st = unit_count % kStages;
                   const uint32_t use = unit_count / kStages;
-                  if (use > 0 && !mbar_wait(&empty[st], (use - 1) & 1, g.status, kErrTimeoutEmpty)) {
+                  if (use > 0 && !mbar_wait(&empty[st], (use - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles)) {
                     alive = false;
                     break;
                   }
@@ -498,14 +500,14 @@ __global__ void __launch_bounds__(kThreads, 1)
       bool alive = true;
       for (uint32_t k = 0;; ++k) {
         const int ts = k % kTupleSlots;
-        if (!mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull)) break;
+        if (!mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles)) break;
         const int64_t t = tslot[ts].t;
         mbar_arrive(&tempty[ts]);
         if (t < 0) break;
         for (int it = 0; it < 3 * npass * ntiles && alive; ++it) {
           const int buf = item_count % K::kNbuf;
           const uint32_t use = item_count / K::kNbuf;
-          if (use > 0 && !mbar_wait(&acce[buf], (use - 1) & 1, g.status, kErrTimeoutAccEmpty)) {
+          if (use > 0 && !mbar_wait(&acce[buf], (use - 1) & 1, g.status, kErrTimeoutAccEmpty, g.wait_cycles)) {
             alive = false;
             break;
           }
@@ -523,14 +525,14 @@ __global__ void __launch_bounds__(kThreads, 1)
               for (int sa = 0; sa < S; ++sa) {
                 if constexpr (MSHARE) {
                   if (sa == 0 &&
-                      !mbar_wait(&mfull[ms], (mcount / kMSlots) & 1, g.status, kErrTimeoutFull)) {
+                      !mbar_wait(&mfull[ms], (mcount / kMSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles)) {
                     alive = false;
                     break;
                   }
                 }
                 const int st = unit_count % kStages;
                 const uint32_t use_s = unit_count / kStages;
-                if (!mbar_wait(&full[st], use_s & 1, g.status, kErrTimeoutFull)) {
+                if (!mbar_wait(&full[st], use_s & 1, g.status, kErrTimeoutFull, g.wait_cycles)) {
                   alive = false;
                   break;
                 }
@@ -607,7 +609,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     bool alive = true;
     for (uint32_t k = 0;; ++k) {
       const int ts = k % kTupleSlots;
-      bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull);
+      bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles);
       const int64_t t = tslot[ts].t;
       // agree on ok so that every epilogue thread leaves (or stays) together
       ok = named_bar_and(1, 128, ok);
@@ -615,13 +617,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!ok || t < 0) break;
       const int wb = k & 1;
       const uint32_t wuse = k >> 1;
-      ok = wuse == 0 || mbar_wait(&wfree[wb], (wuse - 1) & 1, g.status, kErrTimeoutEmpty);
+      ok = wuse == 0 || mbar_wait(&wfree[wb], (wuse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles);
       for (int it = 0; it < 3 * npass * ntiles; ++it) {
         const int gi = it / ntiles, mt = it % ntiles, grp = gi % 3, pass = gi / 3;
         int2 *Wc = reinterpret_cast<int2 *>(Wbase + (size_t)((wb * npass + pass) * 3 + grp) * No3);
         const int buf = item_count % K::kNbuf;
         const uint32_t use = item_count / K::kNbuf;
-        bool okw = ok && alive && mbar_wait(&accf[buf], use & 1, g.status, kErrTimeoutAccFull);
+        bool okw = ok && alive && mbar_wait(&accf[buf], use & 1, g.status, kErrTimeoutAccFull, g.wait_cycles);
         // tcgen05.ld is warp-collective: agree; a failed wait skips the
         // loads but meets the same barriers as the other epilogue warps
         okw = __all_sync(0xffffffffu, okw);
@@ -747,7 +749,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const double inv_unit = 1.0 / g.unit;
     for (uint32_t k = 0;; ++k) {
       const int ts = k % kTupleSlots;
-      bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull);
+      bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles);
       const TupleSlot s = tslot[ts];
       ok = named_bar_and(2, kEnergyThreads, ok);  // leave together
       if (er == 0) mbar_arrive(&tempty[ts]);
@@ -770,7 +772,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       const int wb = k & 1;
-      ok = mbar_wait(&wfull[wb], (k >> 1) & 1, g.status, kErrTimeoutAccFull);
+      ok = mbar_wait(&wfull[wb], (k >> 1) & 1, g.status, kErrTimeoutAccFull, g.wait_cycles);
       double *Wg = Wbase + (size_t)(wb * npass) * 3 * No3;
       const int2 *Wc0 = reinterpret_cast<const int2 *>(Wg);
       const int2 *Wc1 = Wc0 + No3, *Wc2 = Wc1 + No3;
@@ -1432,6 +1434,8 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
   a.jt = 128 / No;
   a.ntiles = (No + a.jt - 1) / a.jt;
   a.prefetch = s.prefetch ? 1 : 0;
+  a.unpublished = s.unpublished ? 1 : 0;
+  a.wait_cycles = s.wait_cycles > 0 ? s.wait_cycles : kWaitCycles;
   a.jt2 = 256 / No;
   a.ntiles2 = (No + a.jt2 - 1) / a.jt2;
   a.nmma = (No * a.jt2 + 15) / 16 * 16;

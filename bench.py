@@ -410,22 +410,39 @@ def run_single(args, workload, world, rank, local):
     kernel_ms = sum(r.device_ms for r in res) / len(res)
     live_fp64 = capi.measure_peaks(local)[0] if (form == "fp64" and rank == 0) else None
     ctx.close()
-    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 3))
+    e2e_steps = 0 if args.no_e2e else args.steps
     pinned, h2d = _pinned(d) if e2e_steps else ({}, sum(
         np.asarray(d[name]).nbytes for name in TENSORS))
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e2e_tuples = 0
-    for s in range(e2e_steps):
+    e2e_tuples, e2e_s, whole = 0, 0.0, None
+    if e2e_steps:
         with capi.Context(No, Nv, local) as c2:
             c2.set_tuning(**tuning_used)
-            for name in TENSORS:
-                c2.upload_ptr(name, pinned[name].data_ptr(), pinned[name].numel(), False)
-            lo, hi = stretch(s)
-            r = c2.run(form=form, slices=slices, use_j=False, first_iteration=lo,
-                       max_iterations=hi - 1)
-            e2e_tuples += r.tuples_done
-    e2e_s = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            for s in range(e2e_steps):
+                # every step: pinned H2D + re-layout of every input (and the
+                # split operands cut again), the step's tuples, energy D2H
+                for name in TENSORS:
+                    c2.upload_ptr(name, pinned[name].data_ptr(), pinned[name].numel(), False)
+                lo, hi = stretch(s)
+                r = c2.run(form=form, slices=slices, use_j=False, first_iteration=lo,
+                           max_iterations=hi - 1)
+                e2e_tuples += r.tuples_done
+            e2e_s = time.perf_counter() - t0
+        # time to E(T) end to end: one context, one upload, the whole list,
+        # where the whole list fits the bench's time budget
+        if time_to_et <= args.whole_list_max_s:
+            t0 = time.perf_counter()
+            with capi.Context(No, Nv, local) as c3:
+                c3.set_tuning(**tuning_used)
+                for name in TENSORS:
+                    c3.upload_ptr(name, pinned[name].data_ptr(), pinned[name].numel(), False)
+                r = c3.run(form=form, slices=slices, use_j=False)
+            secs = time.perf_counter() - t0
+            whole = {"time_to_ET_s": secs, "tflops": n * fpt / secs / 1e12,
+                     "energy": r.energy, "tuples": r.tuples_done,
+                     "note": "context create, pinned H2D + re-layout of all inputs, operands "
+                             "cut, every tuple of the list, E(T) back"}
     e2e_value = (e2e_tuples * fpt / e2e_s / 1e12 * max(world, 1)) if e2e_steps else None
 
     if rank != 0:
@@ -454,9 +471,10 @@ def run_single(args, workload, world, rank, local):
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": 16,
-                "note": "per step: context create, pinned H2D + re-layout of all inputs, "
-                        "split operands cut (split form), the step's tuples, energies D2H"},
+                "d2h_bytes_per_step": 16, "steps": e2e_steps,
+                "note": "per step: pinned H2D + re-layout of all inputs, split operands cut "
+                        "(split form), the step's tuples, energies D2H",
+                "whole_list": whole},
         "clocks": clk,
         "gpu_launches": launches,
     }
@@ -617,6 +635,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--whole-list-max-s", type=float, default=60.0,
+                    help="run the end-to-end whole-list time to E(T) when the device rate "
+                         "says it takes at most this long")
     ap.add_argument("--no", type=int, default=24, help="No of --workload custom")
     ap.add_argument("--nv", type=int, default=240, help="Nv of --workload custom")
     args = ap.parse_args()

@@ -179,6 +179,13 @@ typedef struct {
                             /* S slice units (No % 8 == 0), else variant 2          */
   int32_t split_prefetch;   /* split form: 1 = prefetch the next part's T / V_hhhp  */
                             /* slab tiles into L2 while the current part streams   */
+  int32_t split_wait_kcycles; /* split form: limit of every device-side bounded   */
+                            /* wait in thousands of SM cycles (0 = ~2 s); a wait   */
+                            /* that runs out ends the launch, the run returns      */
+                            /* ATRIP_ERR_TIMEOUT and the context stays usable      */
+  int32_t split_test_unpublished; /* test of that path: 1 = the kernel's producer */
+                            /* publishes no tuple, so every other role's first    */
+                            /* wait runs out (no copy or MMA is issued); 0 = off   */
 } atrip_tuning;
 
 /* Set / read the context's launch parameters (kept until changed). */

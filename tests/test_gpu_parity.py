@@ -30,7 +30,7 @@ def _close(x, y, scale=None):
 
 @pytest.mark.parametrize("name", [n for n in golden_names()
                                   if load_golden(n).get("field", "real") == "real" and
-                                  (load_golden(n)["Nv"] < 200 or load_golden(n)["max_iterations"])])
+                                  (load_golden(n)["Nv"] < 200 or load_golden(n).get("max_iterations"))])
 def test_fp64_matches_reference_fixture(name):
     fx = load_golden(name)
     d = golden_inputs(fx)
