@@ -126,7 +126,7 @@ def _key(ctx: capi.Context, form: str) -> str:
     return f"{_device_name(ctx.device)}|No={ctx.No}|Nv={ctx.Nv}|{form}"
 
 
-def _time(ctx, wins, form, slices, tuning, reps=2):
+def _time(ctx, wins, form, slices, tuning, reps=3):
     ctx.set_tuning(**tuning)
     best = math.inf
     for _ in range(reps):
@@ -139,9 +139,8 @@ def tune_fp64(ctx: capi.Context, flops: float = 2e12, m: int = 8) -> dict:
     n = capi.n_tuples(ctx.Nv)
     wins = windows(n, m, window_size(ctx.No, ctx.Nv, m, flops))
     cands = [{"fp64_tile_rows": 64, "fp64_min_blocks": 0},
-             {"fp64_tile_rows": 64, "fp64_min_blocks": 2}]
-    if ctx.No <= 16:
-        cands.append({"fp64_tile_rows": 32, "fp64_min_blocks": 0})
+             {"fp64_tile_rows": 64, "fp64_min_blocks": 2},
+             {"fp64_tile_rows": 32, "fp64_min_blocks": 0}]
     run_windows(ctx, wins[:1], "fp64")  # warm-up
     timed = [(_time(ctx, wins, "fp64", 0, c), c) for c in cands]
     best_ms, best = min(timed, key=lambda x: x[0])

@@ -92,6 +92,8 @@ struct SplitArgs {
   long long wait_cycles;        // limit of every bounded wait, SM cycles
   int mslot_bytes;              // MSHARE: bytes of one shared M-tile slot
   int nstages;                 // operand ring depth
+  int stage_bytes;             // bytes of one ring stage
+  int b_off;                   // offset of the N-side tile within a stage
   const double *epsi, *epsa, *tai, *Vhh;
   const uint32_t *tuples, *triples;
   const double2 *tri_ef;  // per (i,j,k) triple: (e_i + e_j) + e_k, 2 fac_jk fac_ij
@@ -136,18 +138,42 @@ __global__ void triple_table_kernel(const uint32_t *__restrict__ triples, int n,
 
 __device__ __noinline__ double recip_div(double d) { return 1.0 / d; }
 
-// 1/d for the energy denominators: the FP32 reciprocal of d refined by one
-// Newton-Raphson step, x1 = x0 + x0 (1 - d x0).  With |x0 d - 1| <= ~2^-23
-// the relative error of x1 is about its square (< 2^-44) plus one rounding;
-// outside the FP32 range it falls back to the division (out of line: the
-// orbital-energy gaps never get there).
+// Exact conversions to FP64 done with integer instructions.  The energy
+// warps are bound by this GPU's narrow FP64 pipe; integer operations run
+// beside it.
+// |n| < 2^51: 1.5 2^52 + n has ulp 1, so its bit pattern is that of
+// 1.5 2^52 plus n in the low mantissa bits; subtracting 1.5 2^52 is exact.
+__device__ __forceinline__ double i64_to_f64_exact(long long n) {
+  return __longlong_as_double(0x4338000000000000ll + n) - 6755399441055744.0;
+}
+// Normal FP32 values: same sign and mantissa, exponent rebiased (127 ->
+// 1023); zero, subnormal, infinity and NaN take the conversion instruction.
+__device__ __forceinline__ double f32_to_f64_exact(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                  ((unsigned long long)(e + 896u) << 52) |
+                                  ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+// 1/d for the energy denominators: d truncated to FP32 (integer
+// operations), its FP32 reciprocal (rounded to nearest), widened exactly,
+// refined by one Newton-Raphson step x1 = x0 + x0 (1 - d x0) in FP64.
+// With |x0 d - 1| <= ~1.5 2^-23 the relative error of x1 is about its
+// square (< 2^-44) plus one rounding; outside the FP32 exponent range it
+// falls back to the division (out of line: the orbital-energy gaps never
+// get there).
 __device__ __forceinline__ double recip_nr(double d) {
-  const float df = __double2float_rn(d);
-  const float ad = fabsf(df);
-  if (!(ad > 1e-30f && ad < 1e30f)) return recip_div(d);
-  const double x0 = (double)__frcp_rn(df);
-  const double e = fma(-d, x0, 1.0);
-  return fma(x0, e, x0);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7ffu) - 1023;
+  if (e < -125 || e > 126) return recip_div(d);
+  const uint32_t fb = ((uint32_t)(b >> 32) & 0x80000000u) | ((uint32_t)(e + 127) << 23) |
+                      ((uint32_t)(b >> 29) & 0x7fffffu);
+  const double x0 = f32_to_f64_exact(__frcp_rn(__uint_as_float(fb)));
+  const double err = fma(-d, x0, 1.0);
+  return fma(x0, err, x0);
 }
 
 // dst[s][R][k] (pitch Kp) = sign * digit_s(src(R, k) * scale) for k < K,
@@ -266,21 +292,16 @@ struct KernelShape {
 // Transposed variant: M = 128 rows holding the S slices of the r-column
 // operand stacked (row s No + r), N = nmma <= 256 columns of (p,q) pairs,
 // one 128 x 256 FP32 accumulator per item, double-buffered (all 512 TMEM
-// columns).  Stage: 16 KB M-side tile + 32 KB N-side tile.
+// columns).  The ring stages are sized at launch (t_stage).
 template <int S, bool MSHARE = false>
 struct KernelShapeT {
   static constexpr int kBufCols = 256;
   static constexpr int kNbuf = 2;
   static constexpr int kAllocCols = 512;
-  static constexpr int kBTile = 256 * 128;
-  // MSHARE: the ring holds N-side tiles only; the M-side stacks live in two
-  // separate slots, one per K chunk, shared by its S slice units
-  static constexpr int kStageBytes = (MSHARE ? 0 : kATileBytes) + kBTile;
 };
 constexpr int kMSlots = 2;
 constexpr int kStageCols = 64;   // epilogue staging: 128 rows x 64 FP32 columns,
 constexpr int kStagePitch = 65;  // padded against bank conflicts
-constexpr int kStagingBytes = 128 * kStagePitch * 4;
 
 // Tuple hand-off ring: the producer owns the work queue and publishes each
 // tuple to the MMA issuer, the epilogue warps and the energy warps.
@@ -318,7 +339,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char *ring = smem;
   const int No = g.No, No2 = No * No, No3 = No2 * No;
   const int kStages = g.nstages;
-  unsigned char *mring = ring + kStages * K::kStageBytes;  // MSHARE slots
+  unsigned char *mring = ring + kStages * g.stage_bytes;  // MSHARE slots
   unsigned char *tail = mring + (MSHARE ? kMSlots * g.mslot_bytes : 0);
   // W buffers: [tuple parity][pass] per CTA, pass 1 = J intermediates
   const int npass = g.use_j ? 2 : 1;
@@ -380,7 +401,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   // rows of the A stage tiles past No*jt are never written by TMA: zero them
   for (int i = threadIdx.x;
-       i < (kStages * K::kStageBytes + (MSHARE ? kMSlots * g.mslot_bytes : 0)) / 16;
+       i < (kStages * g.stage_bytes + (MSHARE ? kMSlots * g.mslot_bytes : 0)) / 16;
        i += kThreads)
     reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
   if (warp == 1) {
@@ -397,7 +418,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     // ------------------------------------------------------ TMA producer
     if (lane == 0 && !g.unpublished) {
-      uint32_t unit_count = 0, mcount = 0;
+      uint32_t mcount = 0;
+      int pst = 0;          // ring slot of the next unit
+      uint32_t puse = 0;    // completed passes over the ring
+      unsigned char *sbase = ring;
       bool alive = true;
       for (uint32_t k = 0;; ++k) {
         const int ts = k % kTupleSlots;
@@ -460,13 +484,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                       ++mcount;
                     }
                   }
-                  const int st = unit_count % kStages;
-                  const uint32_t use = unit_count / kStages;
-                  if (use > 0 && !mbar_wait(&empty[st], (use - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles)) {
+                  const int st = pst;
+                  if (puse > 0 && !mbar_wait(&empty[st], (puse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles)) {
                     alive = false;
                     break;
                   }
-                  unsigned char *sbase = ring + st * K::kStageBytes;
                   if constexpr (MSHARE) {
                     mbar_arrive_expect_tx(&full[st], a_bytes);
                     tma_load_5d(sbase, p.amap, &full[st], ch * kKChunk, 0, j0, p.ax, sa);
@@ -476,8 +498,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     // holds level j = sa + sb; N side: (p,q) rows, slice sa
                     mbar_arrive_expect_tx(&full[st], 128 * S * No + a_bytes);
                     tma_load_5d(sbase, p.bmap, &full[st], ch * kKChunk, 0, p.bz, p.by, -sa);
-                    tma_load_5d(sbase + kATileBytes, p.amap, &full[st], ch * kKChunk, 0, j0, p.ax,
-                                sa);
+                    tma_load_5d(sbase + g.b_off, p.amap, &full[st], ch * kKChunk, 0, j0, p.ax, sa);
                   } else {
                     const int nb = S - sa;
                     mbar_arrive_expect_tx(&full[st], a_bytes + nb * NP * 128);
@@ -486,7 +507,13 @@ __global__ void __launch_bounds__(kThreads, 1)
                       tma_load_5d(sbase + kATileBytes + sb * K::kBTile, p.bmap, &full[st],
                                   ch * kKChunk, 0, p.bz, p.by, sb);
                   }
-                  ++unit_count;
+                  if (++pst == kStages) {
+                    pst = 0;
+                    ++puse;
+                    sbase = ring;
+                  } else {
+                    sbase += g.stage_bytes;
+                  }
                 }
             }
           }
@@ -496,7 +523,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == 1) {
     // -------------------------------------------------------- MMA issuer
     if (lane == 0) {
-      uint32_t unit_count = 0, item_count = 0, mcount = 0;
+      // the issuer is a single thread: keep its per-unit work to a few
+      // additions (incremental ring slot, phase and descriptor offset; no
+      // divisions), so the tensor pipe's short instruction queue stays fed
+      uint32_t item_count = 0, mcount = 0;
+      int st = 0;           // ring slot of the next unit
+      uint32_t ph = 0;      // its full-barrier phase parity
+      uint32_t st_off = 0;  // its descriptor offset (bytes >> 4)
+      const uint64_t ring_desc = sdesc_sw128(smem_u32(ring));
+      const uint32_t stage_step = (uint32_t)g.stage_bytes >> 4;
+      const uint32_t b_step = (uint32_t)g.b_off >> 4;
+      const uint32_t id_tv = F16 ? idesc_f16_f32(128, g.nmma) : idesc_bf16_f32(128, g.nmma);
       bool alive = true;
       for (uint32_t k = 0;; ++k) {
         const int ts = k % kTupleSlots;
@@ -530,31 +567,31 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                   }
                 }
-                const int st = unit_count % kStages;
-                const uint32_t use_s = unit_count / kStages;
-                if (!mbar_wait(&full[st], use_s & 1, g.status, kErrTimeoutFull, g.wait_cycles)) {
+                if (!mbar_wait(&full[st], ph, g.status, kErrTimeoutFull, g.wait_cycles)) {
                   alive = false;
                   break;
                 }
                 tc_fence_after();
-                const uint32_t sbase = smem_u32(ring + st * K::kStageBytes);
+                // descriptors: the ring's base descriptor plus the stage
+                // offset (shared-memory addresses stay below 2^18, so the
+                // 14-bit address field never carries)
+                const uint64_t sdesc = ring_desc + st_off;
                 // MSHARE: A = the chunk's shared stack from row block S-1-sa
                 // (No % 8 == 0 keeps the start on a 1024-byte swizzle atom)
                 const uint64_t adesc =
                     MSHARE ? sdesc_sw128(smem_u32(mring + ms * g.mslot_bytes) +
                                          (uint32_t)((S - 1 - sa) * No * 128))
-                           : sdesc_sw128(sbase);
-                const uint64_t bdesc = sdesc_sw128(MSHARE ? sbase : sbase + kATileBytes);
+                           : sdesc;
+                const uint64_t bdesc = sdesc + b_step;
                 // A slice sa against B slices 0 .. S-1-sa in one MMA: the
                 // result columns are the level accumulators sa .. S-1, which
                 // sit side by side in TMEM.  (Transposed variant: the stacked
                 // slices are the M rows, the (p,q) pairs the N columns.)
                 if constexpr (TV) {
-                  const uint32_t id = F16 ? idesc_f16_f32(128, g.nmma) : idesc_bf16_f32(128, g.nmma);
 #pragma unroll
                   for (int kk = 0; kk < kKChunk / 16; ++kk)
                     if (kk < nkk)
-                      mma_bf16(dbase, adesc + 2 * kk, bdesc + 2 * kk, id,
+                      mma_bf16(dbase, adesc + 2 * kk, bdesc + 2 * kk, id_tv,
                                (fresh_main && kk == 0) ? 0u : 1u);
                   fresh_main = false;
                 } else if (SPLIT0 && pt >= 2 && sa == 0) {
@@ -566,7 +603,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                                idesc_bf16_f32(128, NP), (fresh_tr0 && kk == 0) ? 0u : 1u);
                   fresh_tr0 = false;
                   if (S > 1) {
-                    const uint64_t bdesc1 = sdesc_sw128(sbase + kATileBytes + K::kBTile);
+                    const uint64_t bdesc1 = sdesc + ((uint32_t)(kATileBytes + K::kBTile) >> 4);
 #pragma unroll
                     for (int kk = 0; kk < kKChunk / 16; ++kk)
                       if (kk < nkk)
@@ -583,7 +620,13 @@ __global__ void __launch_bounds__(kThreads, 1)
                   fresh_main = false;
                 }
                 mma_commit(&empty[st]);
-                ++unit_count;
+                if (++st == kStages) {
+                  st = 0;
+                  ph ^= 1u;
+                  st_off = 0;
+                } else {
+                  st_off += stage_step;
+                }
                 if constexpr (MSHARE) {
                   if (sa == S - 1) {
                     mma_commit(&mempty[ms]);  // the stack is free once these MMAs end
@@ -644,14 +687,18 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t mno = ((1u << 20) + (uint32_t)No - 1) / (uint32_t)No;
           const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + buf * K::kBufCols;
           for (int c0 = 0; c0 < nvalid && okall; c0 += kStageCols) {
+            // only the S No level rows are staged (rows past them hold
+            // products with whatever follows the stack in shared memory)
             float *row = stg + l * kStagePitch;
 #pragma unroll
             for (int h = 0; h < kStageCols / 16; ++h) {
               float v[16];
               tmem_ld16(tbase + c0 + 16 * h, v);
               tmem_wait_ld();
+              if (l < S * No) {
 #pragma unroll
-              for (int x = 0; x < 16; ++x) row[16 * h + x] = v[x];
+                for (int x = 0; x < 16; ++x) row[16 * h + x] = v[x];
+              }
             }
             named_bar_sync(1, 128);
             // cells (r, column): groups 0 and 1 walk the columns across a
@@ -784,8 +831,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       // level-0 parts: each below 2^24 (BF16 digits) or 2^31 (FP16 digits),
       // so their sum fits int32 or int64 respectively
       auto lev0 = [](int2 c0, int2 c1, int2 c2) {
-        if constexpr (F16) return (double)((long long)c0.x + c1.x + c2.x);
-        else return (double)(c0.x + c1.x + c2.x);
+        return i64_to_f64_exact((long long)c0.x + c1.x + c2.x);
       };
       // four elements per thread in flight: the cells come from L2
       constexpr int kU = 4;
@@ -806,7 +852,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (i < No3) {
             const float rest = (__int_as_float(c[u][0].y) + __int_as_float(c[u][1].y)) +
                                __int_as_float(c[u][2].y);
-            Wd[i] = lev0(c[u][0], c[u][1], c[u][2]) + (double)rest;
+            Wd[i] = lev0(c[u][0], c[u][1], c[u][2]) + f32_to_f64_exact(rest);
           }
         }
       }
@@ -873,7 +919,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int x = i + No * (j + No * kx);
           const int2 c0 = WJ0[x], c1 = WJ1[x], c2 = WJ2[x];
           const float rest = (__int_as_float(c0.y) + __int_as_float(c1.y)) + __int_as_float(c2.y);
-          return lev0(c0, c1, c2) + (double)rest;
+          return lev0(c0, c1, c2) + f32_to_f64_exact(rest);
         });
       }
       if (er == 0) {
@@ -1231,6 +1277,8 @@ int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st
   }
   SplitArgs args = a;
   args.nstages = nst;
+  args.stage_bytes = K::kStageBytes;
+  args.b_off = kATileBytes;
   const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
   auto kern = triples_split_kernel<S, NP, SPLIT0, WSMEM, false>;
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1262,15 +1310,38 @@ size_t mslot_bytes_for(int S, int No) {
   return ((size_t)((S - 1) * No + 128) * 128 + 1023) / 1024 * 1024;
 }
 
+// Epilogue staging of the transposed kernel: the S No level rows of one
+// 64-column round (rows past them are never read).
+size_t staging_bytes_t(int S, int No) {
+  return ((size_t)S * No * kStagePitch * 4 + 15) / 16 * 16;
+}
+
+// One ring stage of the transposed kernel: the M-side stack (S No rows,
+// rounded to a 1024-byte swizzle atom) followed directly by the N-side tile
+// (nmma rows).  The MMA reads 128 stack rows; the rows past S No are the
+// first rows of the N-side tile, which only feed accumulator rows the
+// epilogue never reads.  A stage is at least those 128 rows (16 KB).  With
+// the stacks in their own slots (MSHARE) a stage is the N-side tile alone.
+struct TStage {
+  size_t bytes, b_off;
+};
+TStage t_stage(int S, int No, bool mshare) {
+  const int jt2 = 256 / No;
+  const size_t b = (size_t)((No * jt2 + 15) / 16 * 16) * 128;  // nmma rows, 2 KB multiple
+  if (mshare) return {b, 0};
+  const size_t a = ((size_t)S * No * 128 + 1023) / 1024 * 1024;
+  return {a + b < 16384 ? 16384 : a + b, a};
+}
+
 template <int S, bool WSMEM, bool MSHARE, bool F16>
 int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
-  using K = KernelShapeT<S, MSHARE>;
+  const TStage ts = t_stage(S, a.No, MSHARE);
   const size_t No3 = (size_t)a.No * a.No * a.No;
   const size_t mslots = MSHARE ? kMSlots * mslot_bytes_for(S, a.No) : 0;
-  const size_t vbytes =
-      sizeof(double) * (3 * (size_t)a.No * a.No + (WSMEM ? No3 : 0)) + kStagingBytes + mslots;
+  const size_t vbytes = sizeof(double) * (3 * (size_t)a.No * a.No + (WSMEM ? No3 : 0)) +
+                        staging_bytes_t(S, a.No) + mslots;
   const size_t avail = kSmemLimit - 1024 - kTailBytes - vbytes;
-  int nst = (int)(avail / K::kStageBytes);
+  int nst = (int)(avail / ts.bytes);
   if (nst > kMaxStages) nst = kMaxStages;
   if (p->stage_cap >= 2 && nst > p->stage_cap) nst = p->stage_cap;
   if (nst < 2) {
@@ -1280,7 +1351,9 @@ int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t 
   SplitArgs args = a;
   args.nstages = nst;
   args.mslot_bytes = MSHARE ? (int)mslot_bytes_for(S, a.No) : 0;
-  const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
+  args.stage_bytes = (int)ts.bytes;
+  args.b_off = (int)ts.b_off;
+  const size_t smem = 1024 + (size_t)nst * ts.bytes + kTailBytes + vbytes;
   auto kern = triples_split_kernel<S, 16, false, WSMEM, true, MSHARE, F16>;
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
@@ -1293,26 +1366,27 @@ int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t 
 
 // S slices of No rows fit the 128 M rows, level 0 stays exact (BF16
 // digits, K = 2 (Nv + No) <= 1024) or within int32 (FP16 digits, K < 2048),
-// and two 48 KB operand stages fit next to the singles blocks and staging.
+// and two operand stages fit next to the singles blocks and staging.
 bool transposed_eligible(int S, int No, int Nv, bool f16 = false) {
-  const size_t fixed = 1024 + kTailBytes + kStagingBytes + sizeof(double) * 3 * No * No;
-  return S * No <= 128 && 2 * (Nv + No) <= (f16 ? 2047 : 1024) &&
-         fixed + 2 * (size_t)KernelShapeT<2>::kStageBytes <= (size_t)kSmemLimit;
+  if (S * No > 128 || 2 * (Nv + No) > (f16 ? 2047 : 1024)) return false;
+  const size_t fixed = 1024 + kTailBytes + staging_bytes_t(S, No) + sizeof(double) * 3 * No * No;
+  return fixed + 2 * t_stage(S, No, false).bytes <= (size_t)kSmemLimit;
 }
 
 template <int S, bool F16>
 int launch_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   const size_t No3 = (size_t)a.No * a.No * a.No;
-  const size_t fixed = 1024 + kTailBytes + kStagingBytes + sizeof(double) * 3 * a.No * a.No;
+  const size_t fixed =
+      1024 + kTailBytes + staging_bytes_t(S, a.No) + sizeof(double) * 3 * a.No * a.No;
   // variant 3: one M stack per K chunk shared by the S slice units, where
   // its row blocks start on swizzle atoms (No % 8 == 0) and 2 ring stages fit
   if (p->variant == 3 && a.No % 8 == 0 &&
-      fixed + kMSlots * mslot_bytes_for(S, a.No) + 2 * KernelShapeT<S, true>::kStageBytes <=
+      fixed + kMSlots * mslot_bytes_for(S, a.No) + 2 * t_stage(S, a.No, true).bytes <=
           (size_t)kSmemLimit)
     return launch_shape_t<S, false, true, F16>(p, a, sm_count, st);
-  const bool wsmem =
-      !p->w_global && fixed + sizeof(double) * No3 + 3 * KernelShapeT<S>::kStageBytes <=
-                          (size_t)kSmemLimit;
+  const bool wsmem = !p->w_global && fixed + sizeof(double) * No3 +
+                                         3 * t_stage(S, a.No, false).bytes <=
+                                         (size_t)kSmemLimit;
   return wsmem ? launch_shape_t<S, true, false, F16>(p, a, sm_count, st)
                : launch_shape_t<S, false, false, F16>(p, a, sm_count, st);
 }

@@ -610,6 +610,66 @@ def run_batch96(args, world, rank, local):
     return 0
 
 
+def run_precision_table(args, workload, local):
+    """|dE(T)| and speed of several slice formats on one workload: one
+    context, the FP64 form on 16 evenly spread windows, each split format on
+    the same windows (sampled error, carried to the power-of-two twin) and on
+    one stretch of ~1e14 FP64-equivalent FLOPs (throughput).  One JSON line
+    per format, then a summary line."""
+    from atrip_gb300 import autotune, capi, synth
+
+    No, Nv = WORKLOADS[workload] if workload in WORKLOADS else (args.no, args.nv)
+    fpt = flops_per_tuple(No, Nv)
+    d = synth.make_inputs(No, Nv, SEED)
+    n = capi.n_tuples(Nv)
+    rows = []
+    with capi.Context(No, Nv, local) as ctx:
+        _upload_all(ctx, d)
+        del d
+        m = 16
+        wins = autotune.windows(n, m, autotune.window_size(No, Nv, m, args.compare_flops))
+        autotune.tune(ctx, "fp64", use_cache=not args.retune)
+        ms64, e64 = autotune.run_windows(ctx, wins, "fp64")
+        n_s = sum(hi - lo for lo, hi in wins)
+        fp64_tflops = n_s * fpt / (ms64 * 1e-3) / 1e12
+        batch = max(1, min(n, int(STEP_FLOPS / fpt)))
+        lo = (n - batch) // 2
+        for item in args.precision_table.split(","):
+            form, S = item.split(":")
+            S = int(S)
+            try:
+                tune = autotune.tune(ctx, form, use_cache=not args.retune, slices=S)
+            except capi.AtripError as exc:
+                rows.append({"form": form, "slices": S, "unavailable": str(exc)})
+                print(json.dumps(rows[-1]), flush=True)
+                continue
+            _, es = autotune.run_windows(ctx, wins, form, S)
+            est = autotune.error_estimate(n, e64, es)
+            ctx.run(form=form, slices=S, use_j=False, first_iteration=lo,
+                    max_iterations=lo + batch - 1)  # warm-up
+            r = ctx.run(form=form, slices=S, use_j=False, first_iteration=lo,
+                        max_iterations=lo + batch - 1)
+            tflops = r.tuples_done * fpt / (r.device_ms * 1e-3) / 1e12
+            row = {"workload": f"No={No} Nv={Nv} seed {SEED}", "form": form, "slices": S,
+                   "tflops": tflops, "time_to_ET_s": n * fpt / (tflops * 1e12),
+                   "speedup_vs_fp64": tflops / fp64_tflops, "tuning": tune["tuning"],
+                   "accuracy": {k: est[k] for k in ("E_est", "dE_est", "dE_stderr", "rel",
+                                                    "twin_scale_log2", "twin_E", "twin_dE",
+                                                    "twin_dE_bound", "max_tuple_rel",
+                                                    "sample_tuples")},
+                   "meets_1e-8_Eh_twin": est["twin_dE_bound"] <= args.tol_eh}
+            rows.append(row)
+            print(json.dumps(row), flush=True)
+    print(json.dumps({"precision_table": f"No={No} Nv={Nv}", "fp64_tflops": fp64_tflops,
+                      "fp64_time_to_ET_s": n * fpt / (fp64_tflops * 1e12),
+                      "windows": f"{len(wins)} windows x {wins[0][1] - wins[0][0]} tuples",
+                      "note": "sampled errors: extrapolated from the windows; the estimator's "
+                              "3-sigma bound is checked against whole-list differences at "
+                              "No=24/Nv=240 by tests/test_gpu_cfg2_full.py",
+                      "rows": len(rows)}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -638,6 +698,9 @@ def main():
     ap.add_argument("--whole-list-max-s", type=float, default=60.0,
                     help="run the end-to-end whole-list time to E(T) when the device rate "
                          "says it takes at most this long")
+    ap.add_argument("--precision-table", default="",
+                    help="instead of the bench line: sampled |dE(T)| and speed per slice "
+                         "format, e.g. 'split_f16:2,split_bf16:2,split_bf16:3,split_bf16:4'")
     ap.add_argument("--no", type=int, default=24, help="No of --workload custom")
     ap.add_argument("--nv", type=int, default=240, help="Nv of --workload custom")
     args = ap.parse_args()
@@ -651,6 +714,8 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+    if args.precision_table:
+        return run_precision_table(args, args.workload, local)
     if args.workload == "batch96":
         return run_batch96(args, world, rank, local)
     return run_single(args, args.workload, world, rank, local)

@@ -36,14 +36,23 @@ def test_model_truncation_error(S, bits, bound):
 
 def test_newton_reciprocal_bound():
     """The split kernel's energy denominators use 1/d = x0 + x0 (1 - d x0)
-    with x0 the correctly rounded FP32 reciprocal of FP32(d): emulated here
-    (numpy float32 division rounds to nearest like the FP32 reciprocal
-    instruction), the relative error stays below 2^-44 over the range of
-    orbital-energy gaps and beyond."""
+    with x0 the correctly rounded FP32 reciprocal of d truncated to FP32:
+    emulated here (the truncation on the bit patterns, numpy float32
+    division rounds to nearest like the FP32 reciprocal instruction), the
+    relative error stays below 2^-44 over the range of orbital-energy gaps
+    and beyond."""
     rng = np.random.default_rng(7)
     d = np.concatenate([np.exp(rng.uniform(np.log(1e-6), np.log(1e6), 200000)),
-                        -np.exp(rng.uniform(np.log(1e-3), np.log(1e3), 1000))])
-    x0 = (np.float32(1.0) / d.astype(np.float32)).astype(np.float64)
+                        -np.exp(rng.uniform(np.log(1e-3), np.log(1e3), 1000)),
+                        1.0 + np.arange(1, 4000) * 2.0 ** -40])  # just above powers of two
+    b = d.view(np.uint64)
+    e = ((b >> np.uint64(52)) & np.uint64(0x7ff)).astype(np.int64) - 1023
+    fb = (((b >> np.uint64(32)) & np.uint64(0x80000000)) |
+          (((e + 127).astype(np.uint64)) << np.uint64(23)) |
+          ((b >> np.uint64(29)) & np.uint64(0x7fffff))).astype(np.uint32)
+    d32 = fb.view(np.float32)
+    assert np.all(np.abs(d32.astype(np.float64) - d) <= np.abs(d) * 2.0 ** -23)
+    x0 = (np.float32(1.0) / d32).astype(np.float64)
     e = 1.0 - d * x0  # the kernel forms this with one FMA
     x1 = x0 + x0 * e
     rel = np.abs(x1 * d - 1.0)
