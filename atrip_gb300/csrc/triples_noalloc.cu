@@ -106,8 +106,12 @@ __device__ void build_w(const Args &g, Smem &sm, double *W, const double *Vh, co
       for (int seg = 0; seg < 2; ++seg) {
         const int K = seg == 0 ? (int)Nv : (int)No;
         for (int k0 = 0; k0 < K; k0 += kKC) {
+          // particle rows T[x,E,p,q] are read with consecutive threads on
+          // E (stride Nv), hole rows Vh[p,q,L,w] on p (contiguous): the
+          // nearest addresses this column-major layout offers
           for (int idx = tid; idx < kMT * kKC; idx += kThreads) {
-            const int row = idx % kMT, kk = idx / kMT;
+            const int row = seg == 0 ? idx / kKC : idx % kMT;
+            const int kk = seg == 0 ? idx % kKC : idx / kMT;
             const int64_t m = m0 + row, k = k0 + kk;
             double val = 0.0;
             if (m < No2 && k < K) {
@@ -118,7 +122,9 @@ __device__ void build_w(const Args &g, Smem &sm, double *W, const double *Vh, co
             sm.As[kk][row] = val;
           }
           for (int idx = tid; idx < NC * 8 * kKC; idx += kThreads) {
-            const int col = idx % (NC * 8), kk = idx / (NC * 8);
+            // V_pphp columns Vp[y,z,E,r]: consecutive threads on E (stride Nv^2)
+            const int col = seg == 0 ? idx / kKC : idx % (NC * 8);
+            const int kk = seg == 0 ? idx % kKC : idx / (NC * 8);
             const int64_t k = k0 + kk;
             double val = 0.0;
             if (col < No && k < K) {
