@@ -276,8 +276,9 @@ class Batch:
         return list(res)
 
     def set_tuning(self, **kw) -> None:
-        """FP64 batch-kernel launch parameters (fp64_ctas_per_sm,
-        fp64_min_blocks, tuples_per_claim)."""
+        """Batch launch parameters: FP64 batch kernel (fp64_ctas_per_sm,
+        fp64_min_blocks, tuples_per_claim); split_variant=1 runs the split
+        form as one launch per system instead of one launch for all."""
         t = Tuning()
         for k, v in kw.items():
             setattr(t, k, int(v))

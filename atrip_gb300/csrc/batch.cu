@@ -50,6 +50,8 @@ struct atrip_gpu_batch {
   int64_t graph_launches = 0;
   atrip_tuning tune = {};  // FP64 batch-kernel launch parameters
   int max_per_sm = 1;      // CTAs per SM the workspace is sized for
+  SplitMultiBuffers multi;  // split form: every system in one launch
+  bool multi_used = false;  // the captured graph holds that one launch
 };
 
 namespace {
@@ -233,17 +235,48 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
                                 (uintptr_t)b->tune.fp64_min_blocks,
                                 (uintptr_t)b->tune.tuples_per_claim};
   if (form != ATRIP_FORM_FP64) {
+    // cut every system's operand slices; with one launch for all systems
+    // (the default where one shared-memory layout serves them all) the W
+    // buffers are the batch's own, so the contexts keep minimal ones
+    auto prepare_all = [&](bool one_launch) -> int {
+      for (int k = 0; k < n; ++k) {
+        atrip_gpu_context *c = b->sys[b->order[k]];
+        const TriplesArgs &a = b->h_table[k];
+        c->split.stage_cap = c->tune.split_stages;
+        c->split.w_global = c->tune.split_w_global != 0;
+        c->split.variant = c->tune.split_variant;
+        c->split.prefetch = c->tune.split_prefetch != 0;
+        c->split.f16 = form == ATRIP_FORM_SPLIT_F16;
+        int rc = split_prepare(c->split, c->dt, c->No, c->Nv, one_launch ? 1 : split_ctas(c),
+                               a.use_j != 0, slices, a.triples, a.n_triples, st, &prep_launches);
+        if (rc != ATRIP_OK) return rc;
+      }
+      return ATRIP_OK;
+    };
+    b->multi_used = false;
+    if (b->tune.split_variant != 1) {
+      int rc = prepare_all(true);
+      if (rc != ATRIP_OK) return rc;
+      std::vector<SplitMultiSystem> ms(n);
+      for (int k = 0; k < n; ++k) {
+        atrip_gpu_context *c = b->sys[b->order[k]];
+        const TriplesArgs &a = b->h_table[k];
+        ms[k] = {&c->split, &c->dt, c->No, c->Nv, a.tuples, a.triples, a.n_triples,
+                 a.t_begin, a.t_end, a.use_j != 0, a.e, a.ect};
+      }
+      rc = split_multi_prepare(ms.data(), n, slices, form == ATRIP_FORM_SPLIT_F16, b->sm_count,
+                               b->multi);
+      if (rc == ATRIP_OK) b->multi_used = true;
+      else if (rc != ATRIP_ERR_UNSUPPORTED) return rc;
+      clear_error();
+    }
+    if (!b->multi_used) {
+      const int rc = prepare_all(false);  // one launch per system (batch split_variant 1)
+      if (rc != ATRIP_OK) return rc;
+    }
     for (int k = 0; k < n; ++k) {
       atrip_gpu_context *c = b->sys[b->order[k]];
       const TriplesArgs &a = b->h_table[k];
-      c->split.stage_cap = c->tune.split_stages;
-      c->split.w_global = c->tune.split_w_global != 0;
-      c->split.variant = c->tune.split_variant;
-      c->split.prefetch = c->tune.split_prefetch != 0;
-      c->split.f16 = form == ATRIP_FORM_SPLIT_F16;
-      int rc = split_prepare(c->split, c->dt, c->No, c->Nv, split_ctas(c), a.use_j != 0, slices,
-                             a.triples, a.n_triples, st, &prep_launches);
-      if (rc != ATRIP_OK) return rc;
       const uintptr_t more[] = {(uintptr_t)c->split.generation, (uintptr_t)c->split.impl,
                                 (uintptr_t)a.epsi, (uintptr_t)a.epsa, (uintptr_t)a.tai,
                                 (uintptr_t)a.Vhh, (uintptr_t)a.tuples, (uintptr_t)a.triples,
@@ -255,6 +288,12 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
                                 (uintptr_t)split_ctas(c)};
       key.insert(key.end(), std::begin(more), std::end(more));
     }
+    const uintptr_t more[] = {(uintptr_t)b->multi_used, (uintptr_t)b->multi.smem,
+                              (uintptr_t)b->multi.nstages, (uintptr_t)b->multi.no_lay,
+                              (uintptr_t)b->multi.npass_lay, (uintptr_t)b->multi.wglobal,
+                              (uintptr_t)b->multi.stage_bytes, (uintptr_t)b->multi.wsmem,
+                              (uintptr_t)b->multi.d_desc, (uintptr_t)b->multi.n};
+    key.insert(key.end(), std::begin(more), std::end(more));
     // the split operands were cut on st; the capture stream must see them
     ATRIP_CUDA_TRY(cudaStreamSynchronize(st));
   }
@@ -285,6 +324,12 @@ int atrip_gpu_batch_run(atrip_gpu_batch *b, const atrip_run_options *opts,
                                                    b->stream));
           launches += 1;
         }
+      } else if (b->multi_used) {
+        ATRIP_CUDA_TRY(cudaMemsetAsync(b->multi.d_status, 0, sizeof(int), b->stream));
+        int rc2 = split_multi_enqueue(b->multi, tai_sign, b->sm_count, b->stream, &launches);
+        if (rc2 != ATRIP_OK) return rc2;
+        ATRIP_CUDA_TRY(cudaMemcpyAsync(b->h_status, b->multi.d_status, sizeof(int),
+                                       cudaMemcpyDeviceToHost, b->stream));
       } else {
         for (int k = 0; k < n; ++k) {
           atrip_gpu_context *c = b->sys[b->order[k]];
@@ -371,6 +416,7 @@ int atrip_gpu_batch_destroy(atrip_gpu_batch *b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   destroy_graph(b);
+  split_multi_free(b->multi);
   cudaFreeHost(b->h_table);
   cudaFreeHost(b->h_prefix);
   cudaFreeHost(b->h_sums);

@@ -27,7 +27,7 @@ __global__ void fma_chains(T *out, int iters, T s) {
   if (r == (T)12345.678) out[0] = r;  // keeps the chains live
 }
 
-constexpr int kMmaChains = 8;
+constexpr int kMmaChains = 16;  // as many independent chains as the DFMA loop
 
 __global__ void dmma_chains(double *out, int iters) {
   const double a = threadIdx.x * 1e-3, b = 0.999;

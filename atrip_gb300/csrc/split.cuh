@@ -41,6 +41,42 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
 const int *split_status_ptr(const SplitState &s);
 int split_status_check(int status);
 
+// Several systems (contexts) in ONE persistent launch of the transposed
+// split kernel: a work queue over the concatenation of their tuple ranges,
+// per-system tensor maps and arguments in a device table.  Each system's
+// SplitState must be prepared (split_prepare) with the same slice format.
+struct SplitMultiSystem {
+  SplitState *state;
+  const DeviceTensors *dt;
+  int No, Nv;
+  const uint32_t *tuples, *triples;
+  int n_triples;
+  int64_t t_begin, t_end;
+  bool use_j;
+  double *e, *ect;
+};
+struct SplitMultiBuffers {  // owned by the caller; freed by split_multi_free
+  void *h_desc = nullptr, *d_desc = nullptr;  // descriptor table (pinned host, device)
+  int64_t *h_prefix = nullptr, *d_prefix = nullptr;
+  float *wglobal = nullptr;
+  size_t wglobal_floats = 0;
+  int *d_status = nullptr;
+  unsigned long long *d_queue = nullptr;
+  int cap = 0;  // systems the tables hold
+  // launch layout of the last prepare
+  int n = 0, slices = 0, f16 = 0, no_lay = 0, npass_lay = 1, nstages = 0, wsmem = 0;
+  size_t stage_bytes = 0, smem = 0;
+};
+// Checks the systems fit one launch (the transposed kernel for each, one
+// shared-memory layout), sizes the buffers and fills the host tables.
+// ATRIP_ERR_UNSUPPORTED (no error state kept) when they do not.
+int split_multi_prepare(const SplitMultiSystem *sys, int n, int slices, bool f16, int sm_count,
+                        SplitMultiBuffers &b);
+// Table copies, queue and status reset and the launch, on st (capturable).
+int split_multi_enqueue(const SplitMultiBuffers &b, double tai_sign, int sm_count,
+                        cudaStream_t st, int64_t *launches);
+void split_multi_free(SplitMultiBuffers &b);
+
 // Runs tuples [t_begin, t_end) in the split form, writing e[t], ect[t].
 int split_run(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm_count,
               const uint32_t *tuples, const uint32_t *triples, int n_triples, int64_t t_begin,

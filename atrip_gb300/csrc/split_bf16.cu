@@ -45,6 +45,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -84,12 +85,20 @@ struct SplitMaps {
   CUtensorMap Vp3, TpN3, TpT3, Jp3;
 };
 
+struct SysDesc;
+
 struct SplitArgs {
   int No, Nv, jt, ntiles, kch;  // j per M-tile, M-tiles per group, K chunks of Nv
   int jt2, ntiles2, nmma;       // transposed variant: q per N-tile, N-tiles, MMA N
   int prefetch;                 // 1: L2 prefetch of the next part's (p,q)-row tiles
   int unpublished;              // test: the producer publishes no tuple (waits run out)
   long long wait_cycles;        // limit of every bounded wait, SM cycles
+  // several systems in one launch: per-system descriptors, prefix sums of
+  // their tuple counts (the work queue runs over the concatenation)
+  const SysDesc *sys;
+  const int64_t *prefix;
+  int nsys;
+  int no_lay, npass_lay;  // shared memory / W buffer layout: the largest system
   int mslot_bytes;              // MSHARE: bytes of one shared M-tile slot
   int nstages;                 // operand ring depth
   int stage_bytes;             // bytes of one ring stage
@@ -312,7 +321,94 @@ constexpr int kEnergyThreads = kEnergyWarps * 32;
 struct TupleSlot {
   int64_t t;  // list position, -1 = no more work
   int a, b, c;
+  int s;      // system (multi-system launches), else 0
 };
+
+// One system of a multi-system launch: its tensor maps (global memory) and
+// the arguments that differ between systems.
+struct SysDesc {
+  SplitMaps maps;
+  const double *epsa, *tai, *Vhh;
+  const uint32_t *tuples, *triples;
+  const double2 *tri_ef;
+  double *e, *ect;
+  double unit, unit_j;
+  int64_t t_begin;  // list position of the system's first queued tuple
+  int No, Nv, jt2, ntiles2, nmma, kch, b_off, n_triples, use_j;
+};
+
+// The per-system values of the tuple a role works on: the launch's own
+// arguments, or the tuple's system descriptor.
+struct SysRef {
+  const SplitMaps *maps;
+  const double *epsa, *tai, *Vhh;
+  const uint32_t *tuples, *triples;
+  int64_t t_begin;
+  const double2 *tri_ef;
+  double *e, *ect;
+  double unit, unit_j;
+  int No, Nv, jt, ntiles, kch, nmma, b_off, n_triples, use_j;
+};
+
+template <bool MULTI, bool TV>
+__device__ __forceinline__ SysRef sys_ref(const SplitArgs &g, const SplitMaps &maps, int s) {
+  SysRef r;
+  if constexpr (MULTI) {
+    const SysDesc &d = g.sys[s];
+    r.maps = &d.maps;
+    r.epsa = d.epsa;
+    r.tai = d.tai;
+    r.Vhh = d.Vhh;
+    r.tuples = d.tuples;
+    r.t_begin = d.t_begin;
+    r.triples = d.triples;
+    r.tri_ef = d.tri_ef;
+    r.e = d.e;
+    r.ect = d.ect;
+    r.unit = d.unit;
+    r.unit_j = d.unit_j;
+    r.No = d.No;
+    r.Nv = d.Nv;
+    r.jt = d.jt2;
+    r.ntiles = d.ntiles2;
+    r.kch = d.kch;
+    r.nmma = d.nmma;
+    r.b_off = d.b_off;
+    r.n_triples = d.n_triples;
+    r.use_j = d.use_j;
+  } else {
+    r.maps = &maps;
+    r.epsa = g.epsa;
+    r.tai = g.tai;
+    r.Vhh = g.Vhh;
+    r.tuples = g.tuples;
+    r.t_begin = g.t_begin;
+    r.triples = g.triples;
+    r.tri_ef = g.tri_ef;
+    r.e = g.e;
+    r.ect = g.ect;
+    r.unit = g.unit;
+    r.unit_j = g.unit_j;
+    r.No = g.No;
+    r.Nv = g.Nv;
+    r.jt = TV ? g.jt2 : g.jt;
+    r.ntiles = TV ? g.ntiles2 : g.ntiles;
+    r.kch = g.kch;
+    r.nmma = g.nmma;
+    r.b_off = g.b_off;
+    r.n_triples = g.n_triples;
+    r.use_j = g.use_j;
+  }
+  return r;
+}
+
+// Make a tensor map written to global memory before the launch visible to
+// the bulk-copy engine (multi-system launches keep their maps there).
+__device__ __forceinline__ void tensormap_acquire(const void *map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                   reinterpret_cast<uint64_t>(map))
+               : "memory");
+}
 
 __device__ __forceinline__ int energy_rank(int warp, int lane) {
   return ((warp < 4 ? warp - 2 : warp - 6) << 5) | lane;
@@ -328,7 +424,8 @@ __device__ __forceinline__ int energy_rank(int warp, int lane) {
 // F16 (transposed variant only): FP16 digits of radix 2^11.  Level 0 is
 // then an FP32 sum of products up to 2^20 -- rounded, not exact, but an
 // integer below 2^31 for K < 2048, so the int32 cell format still holds it.
-template <int S, int NP, bool SPLIT0, bool WSMEM, bool TV, bool MSHARE = false, bool F16 = false>
+template <int S, int NP, bool SPLIT0, bool WSMEM, bool TV, bool MSHARE = false, bool F16 = false,
+          bool MULTI = false>
 __global__ void __launch_bounds__(kThreads, 1)
     triples_split_kernel(const __grid_constant__ SplitMaps maps, const SplitArgs g) {
   using K = typename std::conditional<TV, KernelShapeT<S, MSHARE>, KernelShape<S, NP, SPLIT0>>::type;
@@ -337,12 +434,16 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char *ring = smem;
-  const int No = g.No, No2 = No * No, No3 = No2 * No;
+  // layout sizes (the largest system of a multi-system launch); the roles
+  // shadow No, No2, No3 and npass with the values of the tuple at hand
+  const int No = g.no_lay, No2 = No * No, No3 = No2 * No;
+  const size_t WP = (size_t)No3;  // pitch of one group's W cells
   const int kStages = g.nstages;
   unsigned char *mring = ring + kStages * g.stage_bytes;  // MSHARE slots
   unsigned char *tail = mring + (MSHARE ? kMSlots * g.mslot_bytes : 0);
   // W buffers: [tuple parity][pass] per CTA, pass 1 = J intermediates
-  const int npass = g.use_j ? 2 : 1;
+  const int npass = g.npass_lay;
+  const int npL = npass;
   // W buffers: [tuple parity][pass][group] per CTA; each group's items
   // store their contribution to every cell (no read-modify-write), the
   // energy warps add the three groups
@@ -386,6 +487,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&tempty[s], 3);
     }
     fence_mbar_init();
+  }
+  if (threadIdx.x == 0 && !MULTI) {
     prefetch_tensormap(&maps.TaN);
     prefetch_tensormap(&maps.TaT);
     prefetch_tensormap(&maps.VhN);
@@ -412,8 +515,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
-  const int jt = TV ? g.jt2 : g.jt, ntiles = TV ? g.ntiles2 : g.ntiles, kch = g.kch;
-  const int a_bytes = 128 * No * jt;  // full (p,q)-row box, out-of-range rows included
 
   if (warp == 0) {
     // ------------------------------------------------------ TMA producer
@@ -422,6 +523,14 @@ __global__ void __launch_bounds__(kThreads, 1)
       int pst = 0;          // ring slot of the next unit
       uint32_t puse = 0;    // completed passes over the ring
       unsigned char *sbase = ring;
+      // multi-system launch: the system of the previous tuple, its queue
+      // range and values (the positions one CTA draws only grow, so a new
+      // system is looked for only past the end of the current one)
+      int cur = -1;
+      unsigned long long cur_lo = 0, cur_hi = 0;
+      SysRef P = sys_ref<MULTI, TV>(g, maps, 0);
+      const unsigned long long total = MULTI ? (unsigned long long)g.prefix[g.nsys]
+                                             : (unsigned long long)(g.t_end - g.t_begin);
       bool alive = true;
       for (uint32_t k = 0;; ++k) {
         const int ts = k % kTupleSlots;
@@ -429,13 +538,42 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (tuse > 0 && !mbar_wait(&tempty[ts], (tuse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles))
           alive = false;
         const unsigned long long q = alive ? atomicAdd(g.queue, 1ull) : ~0ull;
-        const bool stop = !alive || q >= (unsigned long long)(g.t_end - g.t_begin) ||
-                          *reinterpret_cast<volatile int *>(g.status) != 0;
+        const bool stop = !alive || q >= total || *reinterpret_cast<volatile int *>(g.status) != 0;
         TupleSlot s;
-        s.t = stop ? -1 : g.t_begin + (g.order ? (int64_t)g.order[q] : (int64_t)q);
         s.a = s.b = s.c = 0;
+        s.s = 0;
+        if (stop) {
+          s.t = -1;
+        } else if constexpr (MULTI) {
+          if (q >= cur_hi) {
+            int lo = cur < 0 ? 0 : cur;
+            while (lo + 1 < g.nsys && (unsigned long long)g.prefix[lo + 1] <= q) ++lo;
+            cur = lo;
+            cur_lo = (unsigned long long)g.prefix[lo];
+            cur_hi = (unsigned long long)g.prefix[lo + 1];
+            // first tuple of another system: its values and maps, once
+            P = sys_ref<MULTI, TV>(g, maps, lo);
+            const SplitMaps &M = *P.maps;
+            tensormap_acquire(&M.TaN2);
+            tensormap_acquire(&M.TaT2);
+            tensormap_acquire(&M.VhN2);
+            tensormap_acquire(&M.VhT2);
+            tensormap_acquire(&M.Vp2);
+            tensormap_acquire(&M.TpN2);
+            tensormap_acquire(&M.TpT2);
+            if (P.use_j) {
+              tensormap_acquire(&M.JhN2);
+              tensormap_acquire(&M.JhT2);
+              tensormap_acquire(&M.Jp2);
+            }
+          }
+          s.s = cur;
+          s.t = P.t_begin + (int64_t)(q - cur_lo);
+        } else {
+          s.t = g.t_begin + (g.order ? (int64_t)g.order[q] : (int64_t)q);
+        }
         if (!stop) {
-          const uint32_t pk = g.tuples[s.t];
+          const uint32_t pk = P.tuples[s.t];
           s.a = pk & 0x3ff;
           s.b = (pk >> 10) & 0x3ff;
           s.c = (pk >> 20) & 0x3ff;
@@ -443,11 +581,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         tslot[ts] = s;
         mbar_arrive(&tfull[ts]);  // release: the slot is visible to the waiters
         if (stop) break;
+        // this tuple's system: its sizes (its tensor maps through P.maps)
+        const int No = P.No, jt = P.jt, ntiles = P.ntiles, kch = P.kch;
+        const int npass = P.use_j ? 2 : 1, a_bytes = 128 * No * jt;
         for (int gi = 0; gi < 3 * npass && alive; ++gi)
           for (int mt = 0; mt < ntiles && alive; ++mt) {
             const int j0 = mt * jt, grp = gi % 3, pass = gi / 3;
             for (int pt = 0; pt < 4 && alive; ++pt) {
-              const Part p = part_of(maps, grp, pt, s.a, s.b, s.c, pass, TV);
+              const Part p = part_of(*P.maps, grp, pt, s.a, s.b, s.c, pass, TV);
               const int nch = p.particle ? kch : 1;
               if (g.prefetch) {
                 // the next part of this tuple: its (p,q)-row tiles (the
@@ -457,7 +598,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (npt == 4) { npt = 0; if (++nmt == ntiles) { nmt = 0; ++ngi; } }
                 const int nj0 = nmt * jt;
                 if (ngi < 3 * npass && nj0 + jt <= No) {
-                  const Part np = part_of(maps, ngi % 3, npt, s.a, s.b, s.c, ngi / 3, TV);
+                  const Part np = part_of(*P.maps, ngi % 3, npt, s.a, s.b, s.c, ngi / 3, TV);
                   const int nnch = np.particle ? kch : 1;
                   for (int ch = 0; ch < nnch; ++ch)
                     for (int sa = 0; sa < S; ++sa)
@@ -498,7 +639,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     // holds level j = sa + sb; N side: (p,q) rows, slice sa
                     mbar_arrive_expect_tx(&full[st], 128 * S * No + a_bytes);
                     tma_load_5d(sbase, p.bmap, &full[st], ch * kKChunk, 0, p.bz, p.by, -sa);
-                    tma_load_5d(sbase + g.b_off, p.amap, &full[st], ch * kKChunk, 0, j0, p.ax, sa);
+                    tma_load_5d(sbase + P.b_off, p.amap, &full[st], ch * kKChunk, 0, j0, p.ax, sa);
                   } else {
                     const int nb = S - sa;
                     mbar_arrive_expect_tx(&full[st], a_bytes + nb * NP * 128);
@@ -532,15 +673,23 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t st_off = 0;  // its descriptor offset (bytes >> 4)
       const uint64_t ring_desc = sdesc_sw128(smem_u32(ring));
       const uint32_t stage_step = (uint32_t)g.stage_bytes >> 4;
-      const uint32_t b_step = (uint32_t)g.b_off >> 4;
-      const uint32_t id_tv = F16 ? idesc_f16_f32(128, g.nmma) : idesc_bf16_f32(128, g.nmma);
+      int cur = -1;  // system of the previous tuple (multi-system launch)
+      SysRef P = sys_ref<MULTI, TV>(g, maps, 0);
       bool alive = true;
       for (uint32_t k = 0;; ++k) {
         const int ts = k % kTupleSlots;
         if (!mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles)) break;
         const int64_t t = tslot[ts].t;
+        const int sys = tslot[ts].s;
         mbar_arrive(&tempty[ts]);
         if (t < 0) break;
+        if (MULTI && sys != cur) {  // another system: its values, once
+          cur = sys;
+          P = sys_ref<MULTI, TV>(g, maps, sys);
+        }
+        const int No = P.No, ntiles = P.ntiles, kch = P.kch, npass = P.use_j ? 2 : 1;
+        const uint32_t b_step = (uint32_t)P.b_off >> 4;
+        const uint32_t id_tv = F16 ? idesc_f16_f32(128, P.nmma) : idesc_bf16_f32(128, P.nmma);
         for (int it = 0; it < 3 * npass * ntiles && alive; ++it) {
           const int buf = item_count % K::kNbuf;
           const uint32_t use = item_count / K::kNbuf;
@@ -556,7 +705,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int ch = 0; ch < nch && alive; ++ch) {
               // K steps of 16 that hold data: the zero padding past Nv (last
               // particle chunk) and past No (hole chunk) is skipped
-              const int kvalid = (pt & 1) == 0 ? min(kKChunk, g.Nv - ch * kKChunk) : g.No;
+              const int kvalid = (pt & 1) == 0 ? min(kKChunk, P.Nv - ch * kKChunk) : No;
               const int nkk = (kvalid + 15) / 16;
               const int ms = mcount % kMSlots;
               for (int sa = 0; sa < S; ++sa) {
@@ -649,21 +798,30 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int quarter = warp - 4;
     const int l = quarter * 32 + lane;
     uint32_t item_count = 0;
+    int cur = -1;  // system of the previous tuple (multi-system launch)
+    SysRef P = sys_ref<MULTI, TV>(g, maps, 0);
     bool alive = true;
     for (uint32_t k = 0;; ++k) {
       const int ts = k % kTupleSlots;
       bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles);
       const int64_t t = tslot[ts].t;
+      const int sys = tslot[ts].s;
       // agree on ok so that every epilogue thread leaves (or stays) together
       ok = named_bar_and(1, 128, ok);
       if (threadIdx.x == 128) mbar_arrive(&tempty[ts]);
       if (!ok || t < 0) break;
+      if (MULTI && sys != cur) {  // another system: its values, once
+        cur = sys;
+        P = sys_ref<MULTI, TV>(g, maps, sys);
+      }
+      const int No = P.No, jt = P.jt, ntiles = P.ntiles;
+      const int npass = P.use_j ? 2 : 1;
       const int wb = k & 1;
       const uint32_t wuse = k >> 1;
       ok = wuse == 0 || mbar_wait(&wfree[wb], (wuse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles);
       for (int it = 0; it < 3 * npass * ntiles; ++it) {
         const int gi = it / ntiles, mt = it % ntiles, grp = gi % 3, pass = gi / 3;
-        int2 *Wc = reinterpret_cast<int2 *>(Wbase + (size_t)((wb * npass + pass) * 3 + grp) * No3);
+        int2 *Wc = reinterpret_cast<int2 *>(Wbase + (size_t)((wb * npL + pass) * 3 + grp) * WP);
         const int buf = item_count % K::kNbuf;
         const uint32_t use = item_count / K::kNbuf;
         bool okw = ok && alive && mbar_wait(&accf[buf], use & 1, g.status, kErrTimeoutAccFull, g.wait_cycles);
@@ -789,11 +947,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp < 16) {
     // ------------------------------------------------ energy (10 warps)
     const int er = energy_rank(warp, lane);
-    const int64_t Nv = g.Nv;
-    // W, Z and the singles are carried in units of unit (W cell = level-0
-    // integer + rest), the (cT) T in units of unit_j; both are powers of
-    // two, so the tuple energies scale back exactly at the end
-    const double inv_unit = 1.0 / g.unit;
+    int cur = -1;  // system of the previous tuple (multi-system launch)
+    SysRef P = sys_ref<MULTI, TV>(g, maps, 0);
     for (uint32_t k = 0;; ++k) {
       const int ts = k % kTupleSlots;
       bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles);
@@ -801,17 +956,27 @@ __global__ void __launch_bounds__(kThreads, 1)
       ok = named_bar_and(2, kEnergyThreads, ok);  // leave together
       if (er == 0) mbar_arrive(&tempty[ts]);
       if (!ok || s.t < 0) break;
+      if (MULTI && s.s != cur) {  // another system: its values, once
+        cur = s.s;
+        P = sys_ref<MULTI, TV>(g, maps, s.s);
+      }
+      const int No = P.No, No2 = No * No, No3 = No2 * No;
+      const int64_t Nv = P.Nv;
+      // W, Z and the singles are carried in units of unit (W cell = level-0
+      // integer + rest), the (cT) T in units of unit_j; both are powers of
+      // two, so the tuple energies scale back exactly at the end
+      const double inv_unit = 1.0 / P.unit;
       const int a = s.a, b = s.b, c = s.c;
       if (er < No) {
         // in units of the W cells (a power of two: exact)
-        ta[er] = g.tai_sign * g.tai[a + er * Nv] * inv_unit;
-        tb[er] = g.tai_sign * g.tai[b + er * Nv] * inv_unit;
-        tc[er] = g.tai_sign * g.tai[c + er * Nv] * inv_unit;
+        ta[er] = g.tai_sign * P.tai[a + er * Nv] * inv_unit;
+        tb[er] = g.tai_sign * P.tai[b + er * Nv] * inv_unit;
+        tc[er] = g.tai_sign * P.tai[c + er * Nv] * inv_unit;
       }
       {
-        const double *Vbc = g.Vhh + ((int64_t)b * Nv + c) * No2;
-        const double *Vac = g.Vhh + ((int64_t)a * Nv + c) * No2;
-        const double *Vab = g.Vhh + ((int64_t)a * Nv + b) * No2;
+        const double *Vbc = P.Vhh + ((int64_t)b * Nv + c) * No2;
+        const double *Vac = P.Vhh + ((int64_t)a * Nv + c) * No2;
+        const double *Vab = P.Vhh + ((int64_t)a * Nv + b) * No2;
         for (int i = er; i < No2; i += kEnergyThreads) {
           Vsm[i] = Vbc[i];
           Vsm[No2 + i] = Vac[i];
@@ -820,9 +985,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       const int wb = k & 1;
       ok = mbar_wait(&wfull[wb], (k >> 1) & 1, g.status, kErrTimeoutAccFull, g.wait_cycles);
-      double *Wg = Wbase + (size_t)(wb * npass) * 3 * No3;
+      double *Wg = Wbase + (size_t)(wb * npL) * 3 * WP;
       const int2 *Wc0 = reinterpret_cast<const int2 *>(Wg);
-      const int2 *Wc1 = Wc0 + No3, *Wc2 = Wc1 + No3;
+      const int2 *Wc1 = Wc0 + WP, *Wc2 = Wc1 + WP;
       // W / unit = level-0 integer + rest in FP64 from the three group
       // cells (integer parts exact, rests added in group order): copied into
       // shared memory (the buffers go back to the epilogue at once), or,
@@ -858,13 +1023,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       __threadfence_block();
       named_bar_sync(2, kEnergyThreads);
-      if (WSMEM && !g.use_j && er == 0) mbar_arrive(&wfree[wb]);
+      if (WSMEM && !P.use_j && er == 0) mbar_arrive(&wfree[wb]);
 
       int cls = 0;  // src/atrip/Atrip.cxx:640-642
       if (a == b) cls++;
       if (b == c) cls--;
       const bool distinct = cls == 0;
-      const double epsabc = g.epsa[a] + g.epsa[b] + g.epsa[c];
+      const double epsabc = P.epsa[a] + P.epsa[b] + P.epsa[c];
       const double *Vbc = Vsm, *Vac = Vsm + No2, *Vab = Vsm + 2 * No2;
       auto W = [&](int i, int j, int kx) { return Wd[i + No * (j + No * kx)]; };
       auto Zv = [&](int i, int j, int kx) {
@@ -878,9 +1043,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       // from Tv and Z = W + singles; reduced over the energy warps
       auto tuple_energy = [&](auto &&Tv) {
         double sum = 0.0;
-        for (int n = er; n < g.n_triples && ok; n += kEnergyThreads) {
-          const uint32_t tp = g.triples[n];
-          const double2 ef = g.tri_ef[n];
+        for (int n = er; n < P.n_triples && ok; n += kEnergyThreads) {
+          const uint32_t tp = P.triples[n];
+          const double2 ef = P.tri_ef[n];
           const int i = tp & 0xff, j = (tp >> 8) & 0xff, kx = (tp >> 16) & 0xff;
           const double denominator = epsabc - ef.x;
           double value;
@@ -909,13 +1074,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         named_bar_sync(2, kEnergyThreads);  // red is reused
         return e;
       };
-      const double e = (g.unit * g.unit) * tuple_energy(W);
+      const double e = (P.unit * P.unit) * tuple_energy(W);
       double ect = e;
-      if (g.use_j) {
+      if (P.use_j) {
         // (cT): T from the J pass, Z as above (src/atrip/Atrip.cxx:928-963)
-        const int2 *WJ0 = reinterpret_cast<const int2 *>(Wbase + (size_t)(wb * npass + 1) * 3 * No3);
-        const int2 *WJ1 = WJ0 + No3, *WJ2 = WJ1 + No3;
-        ect = (g.unit * g.unit_j) * tuple_energy([&](int i, int j, int kx) {
+        const int2 *WJ0 = reinterpret_cast<const int2 *>(Wbase + (size_t)(wb * npL + 1) * 3 * WP);
+        const int2 *WJ1 = WJ0 + WP, *WJ2 = WJ1 + WP;
+        ect = (P.unit * P.unit_j) * tuple_energy([&](int i, int j, int kx) {
           const int x = i + No * (j + No * kx);
           const int2 c0 = WJ0[x], c1 = WJ1[x], c2 = WJ2[x];
           const float rest = (__int_as_float(c0.y) + __int_as_float(c1.y)) + __int_as_float(c2.y);
@@ -923,13 +1088,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         });
       }
       if (er == 0) {
-        g.e[s.t] = e;
-        g.ect[s.t] = ect;
+        P.e[s.t] = e;
+        P.ect[s.t] = ect;
       }
       // no zeroing: every group of the next tuple that uses these buffers
       // stores all of its cells
       named_bar_sync(2, kEnergyThreads);  // Wsm is reused by the next tuple
-      if ((!WSMEM || g.use_j) && er == 0) mbar_arrive(&wfree[wb]);
+      if ((!WSMEM || P.use_j) && er == 0) mbar_arrive(&wfree[wb]);
     }
     __syncwarp();
   }
@@ -1412,7 +1577,173 @@ int launch_s(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   return launch_np<S, 64>(p, a, sm_count, st);
 }
 
+// Multi-system launch of the transposed kernel, layout of the largest system.
+template <int S, bool WSMEM, bool F16>
+int launch_multi(const SplitMultiBuffers &b, const SplitArgs &a, int grid, cudaStream_t st) {
+  auto kern = triples_split_kernel<S, 16, false, WSMEM, true, false, F16, true>;
+  ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)b.smem));
+  SplitMaps none;
+  std::memset(&none, 0, sizeof(none));
+  kern<<<grid, kThreads, b.smem, st>>>(none, a);
+  ATRIP_CUDA_TRY(cudaGetLastError());
+  return ATRIP_OK;
+}
+
+template <int S>
+int launch_multi_s(const SplitMultiBuffers &b, const SplitArgs &a, int grid, cudaStream_t st) {
+  if (b.f16) return b.wsmem ? launch_multi<S, true, true>(b, a, grid, st)
+                            : launch_multi<S, false, true>(b, a, grid, st);
+  return b.wsmem ? launch_multi<S, true, false>(b, a, grid, st)
+                 : launch_multi<S, false, false>(b, a, grid, st);
+}
+
 }  // namespace
+
+void split_multi_free(SplitMultiBuffers &b) {
+  cudaFreeHost(b.h_desc);
+  cudaFree(b.d_desc);
+  cudaFreeHost(b.h_prefix);
+  cudaFree(b.d_prefix);
+  cudaFree(b.wglobal);
+  cudaFree(b.d_status);
+  cudaFree(b.d_queue);
+  b = SplitMultiBuffers();
+}
+
+int split_multi_prepare(const SplitMultiSystem *sys, int n, int slices, bool f16, int sm_count,
+                        SplitMultiBuffers &b) {
+  if (n < 1 || slices < 2 || slices > 4 || (f16 && slices != 2)) return ATRIP_ERR_UNSUPPORTED;
+  int no_lay = 0, npass = 1;
+  size_t stage = 0;
+  for (int k = 0; k < n; ++k) {
+    const SplitMultiSystem &m = sys[k];
+    auto *p = static_cast<SplitImpl *>(m.state->impl);
+    if (!m.state->valid || !p || p->S != slices || p->bits != (f16 ? 11 : 8) ||
+        (m.use_j && !p->has_j) || p->tri_n != m.n_triples ||
+        !transposed_eligible(slices, m.No, m.Nv, f16))
+      return ATRIP_ERR_UNSUPPORTED;
+    no_lay = std::max(no_lay, m.No);
+    if (m.use_j) npass = 2;
+    stage = std::max(stage, t_stage(slices, m.No, false).bytes);
+  }
+  const size_t L3 = (size_t)no_lay * no_lay * no_lay;
+  const size_t fixed = 1024 + kTailBytes + staging_bytes_t(slices, no_lay) +
+                       sizeof(double) * 3 * (size_t)no_lay * no_lay;
+  const bool wsmem = fixed + sizeof(double) * L3 + 3 * stage <= (size_t)kSmemLimit;
+  const size_t vfix = fixed + (wsmem ? sizeof(double) * L3 : 0);
+  if (vfix >= (size_t)kSmemLimit) return ATRIP_ERR_UNSUPPORTED;
+  int nst = (int)(((size_t)kSmemLimit - vfix) / stage);
+  if (nst > kMaxStages) nst = kMaxStages;
+  if (nst < 2) return ATRIP_ERR_UNSUPPORTED;
+  // buffers: descriptor tables, prefix sums, W cells of the largest system
+  if (b.cap < n) {
+    cudaFreeHost(b.h_desc);
+    cudaFree(b.d_desc);
+    cudaFreeHost(b.h_prefix);
+    cudaFree(b.d_prefix);
+    b.h_desc = b.d_desc = nullptr;
+    b.h_prefix = b.d_prefix = nullptr;
+    b.cap = 0;
+    ATRIP_CUDA_TRY(cudaMallocHost(&b.h_desc, sizeof(SysDesc) * n));
+    ATRIP_CUDA_TRY(cudaMalloc(&b.d_desc, sizeof(SysDesc) * n));
+    ATRIP_CUDA_TRY(cudaMallocHost(&b.h_prefix, sizeof(int64_t) * (n + 1)));
+    ATRIP_CUDA_TRY(cudaMalloc(&b.d_prefix, sizeof(int64_t) * (n + 1)));
+    b.cap = n;
+  }
+  if (!b.d_status) ATRIP_CUDA_TRY(cudaMalloc(&b.d_status, sizeof(int)));
+  if (!b.d_queue) ATRIP_CUDA_TRY(cudaMalloc(&b.d_queue, sizeof(unsigned long long)));
+  const size_t need = (size_t)sm_count * 2 * npass * 3 * 2 * L3;  // floats
+  if (need > b.wglobal_floats) {
+    cudaFree(b.wglobal);
+    b.wglobal = nullptr;
+    b.wglobal_floats = 0;
+    ATRIP_CUDA_TRY(cudaMalloc(&b.wglobal, sizeof(float) * need));
+    b.wglobal_floats = need;
+  }
+  SysDesc *h = static_cast<SysDesc *>(b.h_desc);
+  b.h_prefix[0] = 0;
+  for (int k = 0; k < n; ++k) {
+    const SplitMultiSystem &m = sys[k];
+    auto *p = static_cast<SplitImpl *>(m.state->impl);
+    SysDesc d;
+    std::memset(&d, 0, sizeof(d));
+    d.maps = p->maps;
+    d.epsa = m.dt->epsa;
+    d.tai = m.dt->tai;
+    d.Vhh = m.dt->Vhh;
+    d.tuples = m.tuples;
+    d.triples = m.triples;
+    d.tri_ef = p->tri_ef;
+    d.e = m.e;
+    d.ect = m.ect;
+    d.unit = p->unit;
+    d.unit_j = p->unit_j;
+    d.t_begin = m.t_begin;
+    d.No = m.No;
+    d.Nv = m.Nv;
+    d.jt2 = 256 / m.No;
+    d.ntiles2 = (m.No + d.jt2 - 1) / d.jt2;
+    d.nmma = (m.No * d.jt2 + 15) / 16 * 16;
+    d.kch = p->Ep / kKChunk;
+    d.b_off = (int)t_stage(slices, m.No, false).b_off;
+    d.n_triples = m.n_triples;
+    d.use_j = m.use_j ? 1 : 0;
+    h[k] = d;
+    b.h_prefix[k + 1] = b.h_prefix[k] + std::max<int64_t>(0, m.t_end - m.t_begin);
+  }
+  b.n = n;
+  b.slices = slices;
+  b.f16 = f16 ? 1 : 0;
+  b.no_lay = no_lay;
+  b.npass_lay = npass;
+  b.nstages = nst;
+  b.wsmem = wsmem ? 1 : 0;
+  b.stage_bytes = stage;
+  b.smem = vfix + (size_t)nst * stage;
+  return ATRIP_OK;
+}
+
+int split_multi_enqueue(const SplitMultiBuffers &b, double tai_sign, int sm_count,
+                        cudaStream_t st, int64_t *launches) {
+  if (b.n < 1) {
+    set_error("split form: multi-system launch not prepared");
+    return ATRIP_ERR_STATE;
+  }
+  ATRIP_CUDA_TRY(cudaMemcpyAsync(b.d_desc, b.h_desc, sizeof(SysDesc) * b.n,
+                                 cudaMemcpyHostToDevice, st));
+  ATRIP_CUDA_TRY(cudaMemcpyAsync(b.d_prefix, b.h_prefix, sizeof(int64_t) * (b.n + 1),
+                                 cudaMemcpyHostToDevice, st));
+  ATRIP_CUDA_TRY(cudaMemsetAsync(b.d_queue, 0, sizeof(unsigned long long), st));
+  ATRIP_CUDA_TRY(cudaMemsetAsync(b.d_status, 0, sizeof(int), st));
+  const int64_t total = b.h_prefix[b.n];
+  if (total == 0) return ATRIP_OK;
+  SplitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.No = b.no_lay;
+  a.nstages = b.nstages;
+  a.stage_bytes = (int)b.stage_bytes;
+  a.tai_sign = tai_sign;
+  a.queue = b.d_queue;
+  a.status = b.d_status;
+  a.wglobal = b.wglobal;
+  a.wait_cycles = kWaitCycles;
+  a.sys = static_cast<const SysDesc *>(b.d_desc);
+  a.prefix = b.d_prefix;
+  a.nsys = b.n;
+  a.no_lay = b.no_lay;
+  a.npass_lay = b.npass_lay;
+  const int grid = (int)std::min<int64_t>(total, sm_count);
+  int rc;
+  switch (b.slices) {
+    case 2: rc = launch_multi_s<2>(b, a, grid, st); break;
+    case 3: rc = launch_multi_s<3>(b, a, grid, st); break;
+    default: rc = launch_multi_s<4>(b, a, grid, st); break;
+  }
+  if (rc != ATRIP_OK) return rc;
+  *launches += 1;
+  return ATRIP_OK;
+}
 
 void split_invalidate(SplitState &s) { s.valid = false; }
 
@@ -1509,6 +1840,11 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
   a.ntiles = (No + a.jt - 1) / a.jt;
   a.prefetch = s.prefetch ? 1 : 0;
   a.unpublished = s.unpublished ? 1 : 0;
+  a.sys = nullptr;
+  a.prefix = nullptr;
+  a.nsys = 0;
+  a.no_lay = No;
+  a.npass_lay = use_j ? 2 : 1;
   a.wait_cycles = s.wait_cycles > 0 ? s.wait_cycles : kWaitCycles;
   a.jt2 = 256 / No;
   a.ntiles2 = (No + a.jt2 - 1) / a.jt2;

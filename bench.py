@@ -292,6 +292,20 @@ def _timed(steps, stream, fn):
     return ms, res, clocks.stop()
 
 
+def _fp64_rate(ctx, n, fpt):
+    """FP64-form TFLOP/s over one contiguous stretch in the middle of the
+    list, 8 waves of the largest resident FP64 grid (4 CTAs per SM) long, so
+    that the last partial wave does not count; the error-sample windows are
+    separate launches too short for a rate (a window of fewer tuples than
+    resident CTAs leaves SMs idle)."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    w = min(n, 8 * 4 * sms)
+    lo = (n - w) // 2
+    r = ctx.run(form="fp64", use_j=False, first_iteration=lo, max_iterations=lo + w - 1)
+    return r.tuples_done * fpt / (r.device_ms * 1e-3) / 1e12, w
+
+
 def _max_over_ranks(world, ms, count):
     if world <= 1:
         return ms, count
@@ -388,14 +402,14 @@ def run_single(args, workload, world, rank, local):
         tuned = ctx.get_tuning()
         fp64_tune = autotune.tune(ctx, "fp64", use_cache=not args.retune)["tuning"]
         ms64, e64 = autotune.run_windows(ctx, wins, "fp64")
+        fp64_tflops, rate_tuples = _fp64_rate(ctx, n, fpt)
         ctx.set_tuning(**tuned)
         ms_s, es = autotune.run_windows(ctx, wins, form, slices)
         est = autotune.error_estimate(n, e64, es)
-        n_s = est["sample_tuples"]
-        fp64_tflops = n_s * fpt / (ms64 * 1e-3) / 1e12
         compare = {"fp64_tflops": fp64_tflops,
                    "fp64_time_to_ET_s": n * fpt / (fp64_tflops * 1e12),
                    "fp64_tuning": fp64_tune,
+                   "fp64_rate_sample": f"{rate_tuples} consecutive tuples mid-list, one launch",
                    "speedup_split_vs_fp64": (n * fpt / (fp64_tflops * 1e12)) / time_to_et,
                    "windows": f"{len(wins)} windows x {wins[0][1] - wins[0][0]} tuples",
                    "accuracy": {k: est[k] for k in ("E_est", "dE_est", "dE_stderr", "rel",
@@ -506,20 +520,28 @@ def run_batch96(args, world, rank, local):
     b = capi.Batch(ctxs)
     btune = autotune.tune_batch(b)
     split_choice = None
+    trials = []
     if form != "fp64":
-        # split kernel variant and processing order for the batch: one full
-        # batch run per candidate, the faster kept
+        # one persistent launch over all systems (the default), or one launch
+        # per system with each system's kernel variant and processing order:
+        # one full batch run per candidate, the faster kept
         base = [c.get_tuning() for c in ctxs]
-        trials = []
-        for cand in ({}, {"split_variant": 2}, {"split_variant": 2, "tuple_block": 4}):
+        bbase = dict(btune["tuning"])
+        for launch, cand in (("one", {}), ("per-system", {}),
+                             ("per-system", {"split_variant": 2}),
+                             ("per-system", {"split_variant": 2, "tuple_block": 4})):
             for c, t in zip(ctxs, base):
                 c.set_tuning(**dict(t, **cand))
+            b.set_tuning(**dict(bbase, split_variant=1 if launch == "per-system" else 0))
             b.run(form=form, slices=slices, use_j=False)  # first run captures the graph
             ms = b.run(form=form, slices=slices, use_j=False)[0].device_ms
-            trials.append((ms, cand))
+            trials.append((ms, dict(cand, launch=launch)))
         split_choice = min(trials, key=lambda x: x[0])
+        cand = {k: v for k, v in split_choice[1].items() if k != "launch"}
         for c, t in zip(ctxs, base):
-            c.set_tuning(**dict(t, **split_choice[1]))
+            c.set_tuning(**dict(t, **cand))
+        b.set_tuning(**dict(bbase, split_variant=1 if split_choice[1]["launch"] == "per-system"
+                            else 0))
     stream = torch.cuda.Stream()
 
     def step(s):
@@ -592,6 +614,8 @@ def run_batch96(args, world, rank, local):
                    "fp64_row_tiles": {"32": tiles.count(32), "64": tiles.count(64)},
                    "batch_tuning": btune["tuning"],
                    "split_tuning": split_choice[1] if split_choice else None,
+                   "split_trials_ms": [(round(t, 2), c) for t, c in trials] if split_choice
+                   else None,
                    "l2": "no flush: inputs > 129 MB L2",
                    "time_to_ET_s": ms / args.steps / 1e3, "input_gen_s": t_gen},
         "compare_fp64": compare,
@@ -630,8 +654,7 @@ def run_precision_table(args, workload, local):
         wins = autotune.windows(n, m, autotune.window_size(No, Nv, m, args.compare_flops))
         autotune.tune(ctx, "fp64", use_cache=not args.retune)
         ms64, e64 = autotune.run_windows(ctx, wins, "fp64")
-        n_s = sum(hi - lo for lo, hi in wins)
-        fp64_tflops = n_s * fpt / (ms64 * 1e-3) / 1e12
+        fp64_tflops, rate_tuples = _fp64_rate(ctx, n, fpt)
         batch = max(1, min(n, int(STEP_FLOPS / fpt)))
         lo = (n - batch) // 2
         for item in args.precision_table.split(","):
@@ -662,6 +685,7 @@ def run_precision_table(args, workload, local):
             print(json.dumps(row), flush=True)
     print(json.dumps({"precision_table": f"No={No} Nv={Nv}", "fp64_tflops": fp64_tflops,
                       "fp64_time_to_ET_s": n * fpt / (fp64_tflops * 1e12),
+                      "fp64_rate_sample": f"{rate_tuples} consecutive tuples mid-list, one launch",
                       "windows": f"{len(wins)} windows x {wins[0][1] - wins[0][0]} tuples",
                       "note": "sampled errors: extrapolated from the windows; the estimator's "
                               "3-sigma bound is checked against whole-list differences at "

@@ -229,11 +229,13 @@ int atrip_gpu_measure_peaks(int32_t device, double *fp64_tflops, double *fp32_tf
  * Batching form: many independent systems in one run.
  *
  * The reference runs one system per Atrip::run (src/atrip/Atrip.cxx:78-1111);
- * a batch replaces a host loop of such calls over small molecules.  The
- * FP64 form runs every system's tuples in ONE persistent launch over a
- * shared device work queue; the split form runs one persistent launch per
- * system.  Either sequence is captured into a CUDA graph on the first run
- * and replayed by later runs with the same form, slice count and range.
+ * a batch replaces a host loop of such calls over small molecules.  Both
+ * forms run every system's tuples in ONE persistent launch over a shared
+ * device work queue (the split form keeps each system's tensor maps in a
+ * device table; where one shared-memory layout cannot serve all systems it
+ * falls back to one launch per system).  The sequence is captured into a
+ * CUDA graph on the first run and replayed by later runs with the same
+ * form, slice count and range.
  *
  * atrip_gpu_batch_create: systems[0..n-1] are contexts on one device with
  * No <= 32; the batch keeps the pointers (destroy the batch before any of
@@ -253,7 +255,8 @@ int atrip_gpu_batch_destroy(atrip_gpu_batch *batch);
 int atrip_gpu_batch_plan(const int32_t *no, const int32_t *nv, int32_t n, int32_t *order);
 /* FP64 launch parameters of the batch kernel (fp64_ctas_per_sm,
  * fp64_min_blocks, tuples_per_claim); the row tile is each context's own
- * fp64_tile_rows and the split fields are each context's own.             */
+ * fp64_tile_rows.  split_variant = 1 runs the split form as one launch per
+ * system (each context's own split fields) instead of one for all.        */
 int atrip_gpu_batch_set_tuning(atrip_gpu_batch *batch, const atrip_tuning *tuning);
 
 /* ---------------------------------------------------------------------

@@ -51,7 +51,11 @@ def _singles(ctxs, **kw):
 @pytest.mark.parametrize("form", ["fp64", "split_bf16", "split_f16"])
 @pytest.mark.parametrize("ijkabc", [False, True])
 def test_batch_matches_single_runs(systems, form, ijkabc):
+    """The split batch is one persistent launch of the transposed kernel over
+    all systems: the single runs use the same kernel (split_variant 2)."""
     ds, ctxs = systems
+    for c in ctxs:
+        c.set_tuning(split_variant=2 if form != "fp64" else 0)
     ref = _singles(ctxs, form=form, ijkabc=ijkabc, use_j=True)
     with capi.Batch(ctxs) as b:
         for rep in range(2):  # the second run replays the captured graph
@@ -66,6 +70,36 @@ def test_batch_matches_single_runs(systems, form, ijkabc):
                 assert abs(r.energy - e0) <= 1e-13 * abs(e0) + 1e-15, (s, r.energy, e0)
                 assert abs(r.ct_energy - ect0) <= 1e-13 * abs(e0) + 1e-15, (s, r.ct_energy, ect0)
             assert res[0].kernel_launches >= 2
+
+
+@pytest.mark.parametrize("form,slices", [("split_f16", 2), ("split_bf16", 3), ("split_bf16", 2)])
+def test_split_batch_one_launch_equals_launch_per_system(systems, form, slices):
+    """All systems in ONE persistent launch (a work queue over their
+    concatenated tuple ranges, per-system tensor maps in a device table)
+    gives the per-tuple energies of one launch per system, bit for bit."""
+    ds, ctxs = systems
+    for c in ctxs:
+        c.set_tuning(split_variant=2)
+    with capi.Batch(ctxs) as b:
+        b.set_tuning(split_variant=1)  # one launch per system
+        per = b.run(form=form, slices=slices, use_j=True)
+        per_e = [c.tuple_energies(0, r.tuples_done) for c, r in zip(ctxs, per)]
+        b.set_tuning()  # default: one launch
+        for rep in range(2):
+            one = b.run(form=form, slices=slices, use_j=True)
+            for s, (c, r, r0) in enumerate(zip(ctxs, one, per)):
+                e, ect = c.tuple_energies(0, r.tuples_done)
+                assert np.array_equal(e, per_e[s][0]), (form, s)
+                assert np.array_equal(ect, per_e[s][1]), (form, s)
+                assert abs(r.energy - r0.energy) <= 1e-14 * abs(r0.energy)
+        # one split launch and one energy reduction, against one per system
+        assert one[0].kernel_launches < per[0].kernel_launches
+    with capi.Batch(ctxs[1:4]) as b:  # a subset and a tuple range
+        r3 = b.run(form=form, slices=slices, use_j=False, first_iteration=5, max_iterations=300)
+        for c, r in zip(ctxs[1:4], r3):
+            one = c.run(form=form, slices=slices, use_j=False, first_iteration=5,
+                        max_iterations=300)
+            assert abs(r.energy - one.energy) <= 1e-13 * abs(one.energy) + 1e-15
 
 
 def test_batch_fp64_matches_oracle(systems):
