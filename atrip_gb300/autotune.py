@@ -155,10 +155,9 @@ def tune_fp64(ctx: capi.Context, flops: float = 2e12, m: int = 8) -> dict:
 
 
 def f16_eligible(No: int, Nv: int) -> bool:
-    """The FP16 form's kernel: 2 slices of No rows in the 128 M rows with two
-    operand stages beside the singles blocks in shared memory (No <= 63),
-    level-0 sums below 2^31 (K = 2 (Nv + No) < 2048)."""
-    return No <= 63 and 2 * (Nv + No) < 2048
+    """The FP16 form's kernel: 2 slices of No rows in the 128 M rows
+    (No <= 64), level-0 sums below 2^31 (K = 2 (Nv + No) < 2048)."""
+    return No <= 64 and 2 * (Nv + No) < 2048
 
 
 def split_formats(No: int, Nv: int, form: str = "split", slice_counts=(2, 3, 4)):

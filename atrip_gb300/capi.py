@@ -29,8 +29,16 @@ EXPORTED = [
     "atrip_gpu_run_fp64_noalloc", "atrip_gpu_batch_create", "atrip_gpu_batch_run",
     "atrip_gpu_batch_destroy", "atrip_gpu_batch_plan", "atrip_gpu_set_tuning",
     "atrip_gpu_get_tuning", "atrip_gpu_batch_set_tuning", "atrip_gpu_last_sums",
-    "atrip_gpu_device_count",
+    "atrip_gpu_device_count", "atrip_gpu_split_profile",
 ]
+
+# counters of atrip_gpu_split_profile, by index
+SPLIT_PROFILE = ("producer_total", "producer_wait_stage", "producer_wait_tuple_slot",
+                 "mma_total", "mma_wait_tuple", "mma_wait_accumulator", "mma_wait_stage",
+                 "epilogue_total", "epilogue_wait_tuple", "epilogue_wait_w_buffer",
+                 "epilogue_wait_accumulator", "energy_total", "energy_wait_tuple",
+                 "energy_wait_w", "energy_w_convert", None, "stages", "tuples", "ctas")
+SPLIT_PROFILE_COUNTERS = 20
 
 
 class AtripError(RuntimeError):
@@ -69,7 +77,7 @@ class Tuning(ctypes.Structure):
                 ("split_w_global", ctypes.c_int32), ("tuple_block", ctypes.c_int32),
                 ("split_variant", ctypes.c_int32), ("split_prefetch", ctypes.c_int32),
                 ("split_wait_kcycles", ctypes.c_int32),
-                ("split_test_unpublished", ctypes.c_int32)]
+                ("split_test_unpublished", ctypes.c_int32), ("split_profile", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -128,6 +136,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.atrip_gpu_batch_set_tuning.argtypes = [P, ctypes.POINTER(Tuning)]
     lib.atrip_gpu_last_sums.argtypes = [P, ctypes.POINTER(ctypes.c_double)]
     lib.atrip_gpu_device_count.argtypes = [ctypes.POINTER(ctypes.c_int32)]
+    lib.atrip_gpu_split_profile.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int32]
     for name in EXPORTED:
         if name not in ("atrip_gpu_n_tuples", "atrip_gpu_last_error", "atrip_gpu_version"):
             getattr(lib, name).restype = ctypes.c_int
@@ -220,6 +229,14 @@ class Context:
         out = (ctypes.c_double * 4)()
         check(self.lib.atrip_gpu_last_sums(self.h, out))
         return tuple(out)
+
+    def split_profile(self) -> dict:
+        """Role profile of the last split run made with tuning
+        split_profile=1: SM cycles per role and wait, summed over CTAs,
+        and the stage / tuple / CTA counts (atrip_gpu_split_profile)."""
+        out = (ctypes.c_uint64 * SPLIT_PROFILE_COUNTERS)()
+        check(self.lib.atrip_gpu_split_profile(self.h, out, SPLIT_PROFILE_COUNTERS))
+        return {name: int(out[k]) for k, name in enumerate(SPLIT_PROFILE) if name}
 
     def tuple_energies(self, t0: int, n: int):
         import numpy as np

@@ -489,6 +489,7 @@ int atrip_gpu_run(atrip_gpu_context *c, const atrip_run_options *opts, atrip_res
       c->split.prefetch = c->tune.split_prefetch != 0;
       c->split.wait_cycles = (long long)c->tune.split_wait_kcycles * 1000;
       c->split.unpublished = c->tune.split_test_unpublished != 0;
+      c->split.profile = c->tune.split_profile != 0;
       c->split.f16 = form == ATRIP_FORM_SPLIT_F16;
       const int ctas = c->tune.split_ctas > 0 ? std::min(c->sm_count, (int)c->tune.split_ctas)
                                               : c->sm_count;
@@ -546,6 +547,8 @@ int atrip_gpu_set_tuning(atrip_gpu_context *c, const atrip_tuning *t) {
   if (t->split_wait_kcycles < 0) return fail(ATRIP_ERR_ARGUMENT, "negative wait limit");
   if (t->split_test_unpublished != 0 && t->split_test_unpublished != 1)
     return fail(ATRIP_ERR_ARGUMENT, "split_test_unpublished must be 0 or 1");
+  if (t->split_profile != 0 && t->split_profile != 1)
+    return fail(ATRIP_ERR_ARGUMENT, "split_profile must be 0 or 1");
   c->tune = *t;
   return ATRIP_OK;
 }
@@ -579,6 +582,15 @@ int atrip_gpu_device_count(int32_t *count) {
   }
   *count = n;
   return ATRIP_OK;
+}
+
+int atrip_gpu_split_profile(const atrip_gpu_context *c, uint64_t *counters, int32_t n) {
+  clear_error();
+  if (!c || !counters || n < ATRIP_SPLIT_PROFILE_COUNTERS)
+    return fail(ATRIP_ERR_ARGUMENT, "need a buffer of ATRIP_SPLIT_PROFILE_COUNTERS counters");
+  cudaSetDevice(c->device);
+  static_assert(sizeof(uint64_t) == sizeof(unsigned long long), "counter width");
+  return split_profile_read(c->split, reinterpret_cast<unsigned long long *>(counters), n);
 }
 
 int atrip_gpu_last_sums(const atrip_gpu_context *c, double *sums) {

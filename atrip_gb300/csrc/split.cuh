@@ -21,9 +21,13 @@ struct SplitState {
   bool f16 = false;         // FP16 digit slices (radix 2^11) instead of BF16 (2^8)
   long long wait_cycles = 0;  // bounded-wait limit in SM cycles (0 = built-in ~2 s)
   bool unpublished = false;   // test: the producer publishes no tuple
+  bool profile = false;       // launch the kernel built with role counters
 };
 
 void split_invalidate(SplitState &s);
+// Role profile of the last profiled launch: the counters listed at
+// atrip_gpu_split_profile (include/atrip_gb300.h), n of them.
+int split_profile_read(const SplitState &s, unsigned long long *out, int n);
 void split_free(SplitState &s);
 
 // Cut the digit slices and build the tensor maps (host work, allocations).
@@ -64,7 +68,7 @@ struct SplitMultiBuffers {  // owned by the caller; freed by split_multi_free
   unsigned long long *d_queue = nullptr;
   int cap = 0;  // systems the tables hold
   // launch layout of the last prepare
-  int n = 0, slices = 0, f16 = 0, no_lay = 0, npass_lay = 1, nstages = 0, wsmem = 0;
+  int n = 0, slices = 0, f16 = 0, no_lay = 0, npass_lay = 1, nstages = 0, wsmem = 0, vsm = 0;
   size_t stage_bytes = 0, smem = 0;
 };
 // Checks the systems fit one launch (the transposed kernel for each, one

@@ -62,7 +62,7 @@ using namespace sm100;
 constexpr int kThreads = 512;
 constexpr int kMaxStages = 6;
 constexpr int kSmemLimit = 232448;  // opt-in dynamic shared memory per block
-constexpr int kTailBytes = 384 + 3 * 64 * 8 + 16 * 8 + 64 * 8;  // + singles blocks (+ W copy)
+constexpr int kTailBytes = 384 + 3 * 64 * 8 + 16 * 8 + 64 * 8;  // + W copy, staging
 constexpr int kKChunk = 64;              // BF16 elements per 128-byte row
 constexpr int kATileBytes = 128 * 128;   // 128 rows x 128 B
 constexpr int kHoleK = 64;               // hole K (L) padded to one chunk
@@ -115,6 +115,8 @@ struct SplitArgs {
   double *e, *ect;
   int *status;
   float *wglobal;  // two W buffers per CTA (one 8-byte cell per element)
+  unsigned long long *prof;  // role profile counters (profiled launches only)
+  int vsm;  // 1: the singles' V_hhpp blocks are copied to shared memory per tuple
 };
 
 // ------------------------------------------------------------------ prep
@@ -410,6 +412,33 @@ __device__ __forceinline__ void tensormap_acquire(const void *map) {
                : "memory");
 }
 
+// Role profile of a launch (kernel instantiations with PROF only): SM cycles
+// each role spends in total and in each of its waits, summed over the CTAs.
+enum ProfSlot {
+  kProfProdTotal, kProfProdEmpty, kProfProdTupleEmpty,
+  kProfMmaTotal, kProfMmaTupleFull, kProfMmaAccEmpty, kProfMmaFull,
+  kProfEpiTotal, kProfEpiTupleFull, kProfEpiWFree, kProfEpiAccFull,
+  kProfEnTotal, kProfEnTupleFull, kProfEnWFull, kProfEnWConvert,
+  kProfUnits = 16, kProfTuples, kProfCtas, kProfSlots = 20
+};
+
+// f() (a bounded wait) with its duration added to acc when PROF.
+template <bool PROF, class F>
+__device__ __forceinline__ bool prof_wait(long long &acc, F f) {
+  if constexpr (PROF) {
+    const long long t = clock64();
+    const bool r = f();
+    acc += clock64() - t;
+    return r;
+  } else {
+    return f();
+  }
+}
+
+__device__ __forceinline__ void prof_add(unsigned long long *prof, int slot, long long v) {
+  atomicAdd(prof + slot, (unsigned long long)v);
+}
+
 __device__ __forceinline__ int energy_rank(int warp, int lane) {
   return ((warp < 4 ? warp - 2 : warp - 6) << 5) | lane;
 }
@@ -425,7 +454,7 @@ __device__ __forceinline__ int energy_rank(int warp, int lane) {
 // then an FP32 sum of products up to 2^20 -- rounded, not exact, but an
 // integer below 2^31 for K < 2048, so the int32 cell format still holds it.
 template <int S, int NP, bool SPLIT0, bool WSMEM, bool TV, bool MSHARE = false, bool F16 = false,
-          bool MULTI = false>
+          bool MULTI = false, bool PROF = false>
 __global__ void __launch_bounds__(kThreads, 1)
     triples_split_kernel(const __grid_constant__ SplitMaps maps, const SplitArgs g) {
   using K = typename std::conditional<TV, KernelShapeT<S, MSHARE>, KernelShape<S, NP, SPLIT0>>::type;
@@ -464,8 +493,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   double *tb = ta + 64;
   double *tc = tb + 64;
   double *red = tc + 64;        // [kEnergyWarps]
-  double *Vsm = red + 16 + 64;  // 3 No x No blocks for the singles
-  double *Wsm = Vsm + 3 * No2;  // FP64 copy of W for the energy loop (WSMEM)
+  double *Vsm = red + 16 + 64;  // the singles' 3 No x No blocks (g.vsm)
+  double *Wsm = Vsm + (g.vsm ? 3 * No2 : 0);  // FP64 copy of W for the energy loop (WSMEM)
   float *stg = reinterpret_cast<float *>(Wsm + (WSMEM ? No3 : 0));  // TV epilogue staging
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -519,6 +548,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     // ------------------------------------------------------ TMA producer
     if (lane == 0 && !g.unpublished) {
+      const long long c_start = PROF ? clock64() : 0;
+      long long c_empty = 0, c_tempty = 0;
       uint32_t mcount = 0;
       int pst = 0;          // ring slot of the next unit
       uint32_t puse = 0;    // completed passes over the ring
@@ -535,7 +566,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (uint32_t k = 0;; ++k) {
         const int ts = k % kTupleSlots;
         const uint32_t tuse = k / kTupleSlots;
-        if (tuse > 0 && !mbar_wait(&tempty[ts], (tuse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles))
+        if (tuse > 0 && !prof_wait<PROF>(c_tempty, [&] {
+              return mbar_wait(&tempty[ts], (tuse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles);
+            }))
           alive = false;
         const unsigned long long q = alive ? atomicAdd(g.queue, 1ull) : ~0ull;
         const bool stop = !alive || q >= total || *reinterpret_cast<volatile int *>(g.status) != 0;
@@ -626,7 +659,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                     }
                   }
                   const int st = pst;
-                  if (puse > 0 && !mbar_wait(&empty[st], (puse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles)) {
+                  if (puse > 0 && !prof_wait<PROF>(c_empty, [&] {
+                        return mbar_wait(&empty[st], (puse - 1) & 1, g.status, kErrTimeoutEmpty,
+                                         g.wait_cycles);
+                      })) {
                     alive = false;
                     break;
                   }
@@ -659,6 +695,12 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
       }
+      if constexpr (PROF) {
+        prof_add(g.prof, kProfProdTotal, clock64() - c_start);
+        prof_add(g.prof, kProfProdEmpty, c_empty);
+        prof_add(g.prof, kProfProdTupleEmpty, c_tempty);
+        prof_add(g.prof, kProfCtas, 1);
+      }
     }
     __syncwarp();
   } else if (warp == 1) {
@@ -667,6 +709,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       // the issuer is a single thread: keep its per-unit work to a few
       // additions (incremental ring slot, phase and descriptor offset; no
       // divisions), so the tensor pipe's short instruction queue stays fed
+      const long long c_start = PROF ? clock64() : 0;
+      long long c_tfull = 0, c_acce = 0, c_full = 0, n_units = 0, n_tuples = 0;
       uint32_t item_count = 0, mcount = 0;
       int st = 0;           // ring slot of the next unit
       uint32_t ph = 0;      // its full-barrier phase parity
@@ -678,11 +722,16 @@ __global__ void __launch_bounds__(kThreads, 1)
       bool alive = true;
       for (uint32_t k = 0;; ++k) {
         const int ts = k % kTupleSlots;
-        if (!mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles)) break;
+        if (!prof_wait<PROF>(c_tfull, [&] {
+              return mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull,
+                               g.wait_cycles);
+            }))
+          break;
         const int64_t t = tslot[ts].t;
         const int sys = tslot[ts].s;
         mbar_arrive(&tempty[ts]);
         if (t < 0) break;
+        ++n_tuples;
         if (MULTI && sys != cur) {  // another system: its values, once
           cur = sys;
           P = sys_ref<MULTI, TV>(g, maps, sys);
@@ -693,7 +742,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int it = 0; it < 3 * npass * ntiles && alive; ++it) {
           const int buf = item_count % K::kNbuf;
           const uint32_t use = item_count / K::kNbuf;
-          if (use > 0 && !mbar_wait(&acce[buf], (use - 1) & 1, g.status, kErrTimeoutAccEmpty, g.wait_cycles)) {
+          if (use > 0 && !prof_wait<PROF>(c_acce, [&] {
+                return mbar_wait(&acce[buf], (use - 1) & 1, g.status, kErrTimeoutAccEmpty,
+                                 g.wait_cycles);
+              })) {
             alive = false;
             break;
           }
@@ -716,7 +768,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                   }
                 }
-                if (!mbar_wait(&full[st], ph, g.status, kErrTimeoutFull, g.wait_cycles)) {
+                ++n_units;
+                if (!prof_wait<PROF>(c_full, [&] {
+                      return mbar_wait(&full[st], ph, g.status, kErrTimeoutFull, g.wait_cycles);
+                    })) {
                   alive = false;
                   break;
                 }
@@ -790,6 +845,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         if (!alive) break;
       }
+      if constexpr (PROF) {
+        prof_add(g.prof, kProfMmaTotal, clock64() - c_start);
+        prof_add(g.prof, kProfMmaTupleFull, c_tfull);
+        prof_add(g.prof, kProfMmaAccEmpty, c_acce);
+        prof_add(g.prof, kProfMmaFull, c_full);
+        prof_add(g.prof, kProfUnits, n_units);
+        prof_add(g.prof, kProfTuples, n_tuples);
+      }
     }
     __syncwarp();
   } else if (warp >= 4 && warp < 8) {
@@ -797,13 +860,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     // warp % 4 selects the 32-lane TMEM quarter this warp may read
     const int quarter = warp - 4;
     const int l = quarter * 32 + lane;
+    const long long c_start = PROF ? clock64() : 0;
+    long long c_tfull = 0, c_wfree = 0, c_accf = 0;
     uint32_t item_count = 0;
     int cur = -1;  // system of the previous tuple (multi-system launch)
     SysRef P = sys_ref<MULTI, TV>(g, maps, 0);
     bool alive = true;
     for (uint32_t k = 0;; ++k) {
       const int ts = k % kTupleSlots;
-      bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles);
+      bool ok = prof_wait<PROF>(c_tfull, [&] {
+        return mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles);
+      });
       const int64_t t = tslot[ts].t;
       const int sys = tslot[ts].s;
       // agree on ok so that every epilogue thread leaves (or stays) together
@@ -818,13 +885,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int npass = P.use_j ? 2 : 1;
       const int wb = k & 1;
       const uint32_t wuse = k >> 1;
-      ok = wuse == 0 || mbar_wait(&wfree[wb], (wuse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles);
+      ok = wuse == 0 || prof_wait<PROF>(c_wfree, [&] {
+             return mbar_wait(&wfree[wb], (wuse - 1) & 1, g.status, kErrTimeoutEmpty, g.wait_cycles);
+           });
       for (int it = 0; it < 3 * npass * ntiles; ++it) {
         const int gi = it / ntiles, mt = it % ntiles, grp = gi % 3, pass = gi / 3;
         int2 *Wc = reinterpret_cast<int2 *>(Wbase + (size_t)((wb * npL + pass) * 3 + grp) * WP);
         const int buf = item_count % K::kNbuf;
         const uint32_t use = item_count / K::kNbuf;
-        bool okw = ok && alive && mbar_wait(&accf[buf], use & 1, g.status, kErrTimeoutAccFull, g.wait_cycles);
+        bool okw = ok && alive && prof_wait<PROF>(c_accf, [&] {
+                     return mbar_wait(&accf[buf], use & 1, g.status, kErrTimeoutAccFull, g.wait_cycles);
+                   });
         // tcgen05.ld is warp-collective: agree; a failed wait skips the
         // loads but meets the same barriers as the other epilogue warps
         okw = __all_sync(0xffffffffu, okw);
@@ -862,31 +933,44 @@ __global__ void __launch_bounds__(kThreads, 1)
             // cells (r, column): groups 0 and 1 walk the columns across a
             // warp (W index consecutive in p), group 2 walks r (its W index
             // is consecutive in r), so every warp store coalesces
-            const int ncells = No * kStageCols;
-            for (int id = t128; id < ncells; id += 128) {
-              int r, ccu;
-              if (grp == 2) {
-                ccu = (int)(((uint32_t)id * mno) >> 20);
-                r = id - ccu * No;
-              } else {
-                r = rq + 2 * ((id - t128) >> 7);
-                ccu = cc;
-              }
-              const int n = c0 + ccu;
-              if (n >= nvalid) continue;
-              const int lev0 = __float2int_rn(stg[r * kStagePitch + ccu]);
-              float rr = 0.f;
+            if (grp != 2) {
+              // one column per thread, rows rq, rq + 2, ...: the column's
+              // (p, q) and the W index of row 0 once, then a fixed stride
+              const int n = c0 + cc;
+              if (n < nvalid) {
+                const int nq = (int)(((uint32_t)n * mno) >> 20);
+                const int f = n - nq * No, sl = q0 + nq;
+                // group 0: (i, j, k) = (f, sl, r); group 1: (f, r, sl)
+                const int base = grp == 0 ? f + No * sl : f + No * No * sl;
+                const int rstep = grp == 0 ? No * No : No;
+                const float *col = stg + cc;
+                for (int r = rq; r < No; r += 2) {
+                  const int lev0 = __float2int_rn(col[r * kStagePitch]);
+                  float rr = 0.f;
 #pragma unroll
-              for (int q = S - 1; q >= 1; --q)
-                rr = rr * kInvRadix + stg[(q * No + r) * kStagePitch + ccu];
-              const int nq = (int)(((uint32_t)n * mno) >> 20);
-              const int f = n - nq * No, sl = q0 + nq;
-              int i, jj, kx;
-              if (grp == 0) { i = f; jj = sl; kx = r; }
-              else if (grp == 1) { i = f; kx = sl; jj = r; }
-              else { jj = f; kx = sl; i = r; }
-              __stcg(&Wc[i + No * (jj + No * kx)],
-                     make_int2(lev0, __float_as_int(rr * kInvRadix)));
+                  for (int q = S - 1; q >= 1; --q)
+                    rr = rr * kInvRadix + col[(q * No + r) * kStagePitch];
+                  __stcg(&Wc[base + r * rstep], make_int2(lev0, __float_as_int(rr * kInvRadix)));
+                }
+              }
+            } else {
+              const int ncells = No * kStageCols;
+              for (int id = t128; id < ncells; id += 128) {
+                const int ccu = (int)(((uint32_t)id * mno) >> 20);
+                const int r = id - ccu * No;
+                const int n = c0 + ccu;
+                if (n >= nvalid) continue;
+                const int lev0 = __float2int_rn(stg[r * kStagePitch + ccu]);
+                float rr = 0.f;
+#pragma unroll
+                for (int q = S - 1; q >= 1; --q)
+                  rr = rr * kInvRadix + stg[(q * No + r) * kStagePitch + ccu];
+                const int nq = (int)(((uint32_t)n * mno) >> 20);
+                const int f = n - nq * No, sl = q0 + nq;
+                // group 2: (i, j, k) = (r, f, sl)
+                __stcg(&Wc[r + No * (f + No * sl)],
+                       make_int2(lev0, __float_as_int(rr * kInvRadix)));
+              }
             }
             named_bar_sync(1, 128);  // the staging buffer is reused
           }
@@ -943,15 +1027,25 @@ __global__ void __launch_bounds__(kThreads, 1)
       named_bar_sync(1, 128);
       if (threadIdx.x == 128) mbar_arrive(&wfull[wb]);
     }
+    if (PROF && threadIdx.x == 128) {
+      prof_add(g.prof, kProfEpiTotal, clock64() - c_start);
+      prof_add(g.prof, kProfEpiTupleFull, c_tfull);
+      prof_add(g.prof, kProfEpiWFree, c_wfree);
+      prof_add(g.prof, kProfEpiAccFull, c_accf);
+    }
     __syncwarp();
   } else if (warp < 16) {
     // ------------------------------------------------ energy (10 warps)
     const int er = energy_rank(warp, lane);
+    const long long c_start = PROF ? clock64() : 0;
+    long long c_tfull = 0, c_wfull = 0, c_conv = 0, c_t0 = 0;
     int cur = -1;  // system of the previous tuple (multi-system launch)
     SysRef P = sys_ref<MULTI, TV>(g, maps, 0);
     for (uint32_t k = 0;; ++k) {
       const int ts = k % kTupleSlots;
-      bool ok = mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles);
+      bool ok = prof_wait<PROF>(c_tfull, [&] {
+        return mbar_wait(&tfull[ts], (k / kTupleSlots) & 1, g.status, kErrTimeoutFull, g.wait_cycles);
+      });
       const TupleSlot s = tslot[ts];
       ok = named_bar_and(2, kEnergyThreads, ok);  // leave together
       if (er == 0) mbar_arrive(&tempty[ts]);
@@ -973,7 +1067,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         tb[er] = g.tai_sign * P.tai[b + er * Nv] * inv_unit;
         tc[er] = g.tai_sign * P.tai[c + er * Nv] * inv_unit;
       }
-      {
+      if (g.vsm) {
+        // the singles' blocks into shared memory while the MMAs of this
+        // tuple run (visible to all after the W conversion's barrier)
         const double *Vbc = P.Vhh + ((int64_t)b * Nv + c) * No2;
         const double *Vac = P.Vhh + ((int64_t)a * Nv + c) * No2;
         const double *Vab = P.Vhh + ((int64_t)a * Nv + b) * No2;
@@ -984,7 +1080,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       const int wb = k & 1;
-      ok = mbar_wait(&wfull[wb], (k >> 1) & 1, g.status, kErrTimeoutAccFull, g.wait_cycles);
+      ok = prof_wait<PROF>(c_wfull, [&] {
+        return mbar_wait(&wfull[wb], (k >> 1) & 1, g.status, kErrTimeoutAccFull, g.wait_cycles);
+      });
+      if constexpr (PROF) c_t0 = clock64();
       double *Wg = Wbase + (size_t)(wb * npL) * 3 * WP;
       const int2 *Wc0 = reinterpret_cast<const int2 *>(Wg);
       const int2 *Wc1 = Wc0 + WP, *Wc2 = Wc1 + WP;
@@ -999,7 +1098,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         return i64_to_f64_exact((long long)c0.x + c1.x + c2.x);
       };
       // four elements per thread in flight: the cells come from L2
-      constexpr int kU = 4;
+      constexpr int kU = 6;
       for (int i0 = er; i0 < No3; i0 += kU * kEnergyThreads) {
         int2 c[kU][3];
 #pragma unroll
@@ -1023,6 +1122,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       __threadfence_block();
       named_bar_sync(2, kEnergyThreads);
+      if constexpr (PROF) c_conv += clock64() - c_t0;
       if (WSMEM && !P.use_j && er == 0) mbar_arrive(&wfree[wb]);
 
       int cls = 0;  // src/atrip/Atrip.cxx:640-642
@@ -1030,7 +1130,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (b == c) cls--;
       const bool distinct = cls == 0;
       const double epsabc = P.epsa[a] + P.epsa[b] + P.epsa[c];
-      const double *Vbc = Vsm, *Vac = Vsm + No2, *Vab = Vsm + 2 * No2;
+      // the singles' No x No blocks of V_hhpp: the shared copy, or read in
+      // place (L1 / L2) where shared memory is left to the operand ring
+      const double *Vbc = g.vsm ? Vsm : P.Vhh + ((int64_t)b * Nv + c) * No2;
+      const double *Vac = g.vsm ? Vsm + No2 : P.Vhh + ((int64_t)a * Nv + c) * No2;
+      const double *Vab = g.vsm ? Vsm + 2 * No2 : P.Vhh + ((int64_t)a * Nv + b) * No2;
       auto W = [&](int i, int j, int kx) { return Wd[i + No * (j + No * kx)]; };
       auto Zv = [&](int i, int j, int kx) {
         double z = W(i, j, kx);
@@ -1096,6 +1200,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       named_bar_sync(2, kEnergyThreads);  // Wsm is reused by the next tuple
       if ((!WSMEM || P.use_j) && er == 0) mbar_arrive(&wfree[wb]);
     }
+    if (PROF && er == 0) {
+      prof_add(g.prof, kProfEnTotal, clock64() - c_start);
+      prof_add(g.prof, kProfEnTupleFull, c_tfull);
+      prof_add(g.prof, kProfEnWFull, c_wfull);
+      prof_add(g.prof, kProfEnWConvert, c_conv);
+    }
     __syncwarp();
   }
 
@@ -1125,6 +1235,7 @@ struct SplitImpl {
   int bits = 8;       // digit radix 2^bits: 8 = BF16 slices, 11 = FP16 slices
   double2 *tri_ef = nullptr;  // per-triple denominator part and weight
   int tri_n = 0;
+  unsigned long long *d_prof = nullptr;  // role profile of the last profiled launch
   SplitMaps maps;
 };
 
@@ -1143,6 +1254,7 @@ void free_impl(SplitImpl *p) {
   cudaFree(p->wglobal);
   cudaFree(p->d_status);
   cudaFree(p->tri_ef);
+  cudaFree(p->d_prof);
   delete p;
 }
 
@@ -1431,7 +1543,11 @@ template <int S, int NP, bool SPLIT0, bool WSMEM>
 int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   using K = KernelShape<S, NP, SPLIT0>;
   const size_t No3 = (size_t)a.No * a.No * a.No;
-  const size_t vbytes = sizeof(double) * (3 * (size_t)a.No * a.No + (WSMEM ? No3 : 0));
+  const size_t vsm_bytes = sizeof(double) * 3 * (size_t)a.No * a.No;
+  size_t vbytes = sizeof(double) * (WSMEM ? No3 : 0);
+  // the singles' blocks go to shared memory where three stages still fit
+  const bool vsm = kSmemLimit - 1024 - kTailBytes - vbytes >= vsm_bytes + 3 * K::kStageBytes;
+  if (vsm) vbytes += vsm_bytes;
   const size_t avail = kSmemLimit - 1024 - kTailBytes - vbytes;
   int nst = (int)(avail / K::kStageBytes);
   if (nst > kMaxStages) nst = kMaxStages;
@@ -1444,6 +1560,7 @@ int launch_shape(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st
   args.nstages = nst;
   args.stage_bytes = K::kStageBytes;
   args.b_off = kATileBytes;
+  args.vsm = vsm ? 1 : 0;
   const size_t smem = 1024 + (size_t)nst * K::kStageBytes + kTailBytes + vbytes;
   auto kern = triples_split_kernel<S, NP, SPLIT0, WSMEM, false>;
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1503,8 +1620,12 @@ int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t 
   const TStage ts = t_stage(S, a.No, MSHARE);
   const size_t No3 = (size_t)a.No * a.No * a.No;
   const size_t mslots = MSHARE ? kMSlots * mslot_bytes_for(S, a.No) : 0;
-  const size_t vbytes = sizeof(double) * (3 * (size_t)a.No * a.No + (WSMEM ? No3 : 0)) +
-                        staging_bytes_t(S, a.No) + mslots;
+  const size_t vsm_bytes = sizeof(double) * 3 * (size_t)a.No * a.No;
+  size_t vbytes = sizeof(double) * (WSMEM ? No3 : 0) + staging_bytes_t(S, a.No) + mslots;
+  // the singles' blocks go to shared memory where three stages still fit
+  // beside them (at No = 56 they would leave two)
+  const bool vsm = kSmemLimit - 1024 - kTailBytes - vbytes >= vsm_bytes + 3 * ts.bytes;
+  if (vsm) vbytes += vsm_bytes;
   const size_t avail = kSmemLimit - 1024 - kTailBytes - vbytes;
   int nst = (int)(avail / ts.bytes);
   if (nst > kMaxStages) nst = kMaxStages;
@@ -1518,8 +1639,18 @@ int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t 
   args.mslot_bytes = MSHARE ? (int)mslot_bytes_for(S, a.No) : 0;
   args.stage_bytes = (int)ts.bytes;
   args.b_off = (int)ts.b_off;
+  args.vsm = vsm ? 1 : 0;
   const size_t smem = 1024 + (size_t)nst * ts.bytes + kTailBytes + vbytes;
   auto kern = triples_split_kernel<S, 16, false, WSMEM, true, MSHARE, F16>;
+  if (a.prof) {
+    // the role profile is built for the two-slice transposed kernel only
+    if constexpr (S == 2 && !MSHARE) {
+      kern = triples_split_kernel<S, 16, false, WSMEM, true, false, F16, false, true>;
+    } else {
+      set_error("split form: the role profile needs 2 slices and the transposed kernel (variant 2)");
+      return ATRIP_ERR_UNSUPPORTED;
+    }
+  }
   ATRIP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   const int64_t n = a.t_end - a.t_begin;
@@ -1531,10 +1662,10 @@ int launch_shape_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t 
 
 // S slices of No rows fit the 128 M rows, level 0 stays exact (BF16
 // digits, K = 2 (Nv + No) <= 1024) or within int32 (FP16 digits, K < 2048),
-// and two operand stages fit next to the singles blocks and staging.
+// and two operand stages fit next to the epilogue staging.
 bool transposed_eligible(int S, int No, int Nv, bool f16 = false) {
   if (S * No > 128 || 2 * (Nv + No) > (f16 ? 2047 : 1024)) return false;
-  const size_t fixed = 1024 + kTailBytes + staging_bytes_t(S, No) + sizeof(double) * 3 * No * No;
+  const size_t fixed = 1024 + kTailBytes + staging_bytes_t(S, No);
   return fixed + 2 * t_stage(S, No, false).bytes <= (size_t)kSmemLimit;
 }
 
@@ -1542,7 +1673,7 @@ template <int S, bool F16>
 int launch_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   const size_t No3 = (size_t)a.No * a.No * a.No;
   const size_t fixed =
-      1024 + kTailBytes + staging_bytes_t(S, a.No) + sizeof(double) * 3 * a.No * a.No;
+      1024 + kTailBytes + staging_bytes_t(S, a.No);
   // variant 3: one M stack per K chunk shared by the S slice units, where
   // its row blocks start on swizzle atoms (No % 8 == 0) and 2 ring stages fit
   if (p->variant == 3 && a.No % 8 == 0 &&
@@ -1559,7 +1690,7 @@ int launch_t(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
 // FP16 digits: the transposed kernel only (variant 3 where chosen).
 int launch_f16(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   if (p->S != 2 || !transposed_eligible(2, a.No, a.Nv, true)) {
-    set_error("split FP16 form: needs 2 slices, No <= 63 and 2 (Nv + No) < 2048 (No=" +
+    set_error("split FP16 form: needs 2 slices, No <= 64 and 2 (Nv + No) < 2048 (No=" +
               std::to_string(a.No) + ", Nv=" + std::to_string(a.Nv) + ")");
     return ATRIP_ERR_UNSUPPORTED;
   }
@@ -1570,6 +1701,10 @@ template <int S>
 int launch_s(SplitImpl *p, const SplitArgs &a, int sm_count, cudaStream_t st) {
   if (p->variant >= 2 && transposed_eligible(S, a.No, a.Nv))
     return launch_t<S, false>(p, a, sm_count, st);
+  if (a.prof) {
+    set_error("split form: the role profile needs 2 slices and the transposed kernel (variant 2)");
+    return ATRIP_ERR_UNSUPPORTED;
+  }
   const int No = a.No;
   if (No <= 16) return launch_np<S, 16>(p, a, sm_count, st);
   if (No <= 32) return launch_np<S, 32>(p, a, sm_count, st);
@@ -1628,10 +1763,12 @@ int split_multi_prepare(const SplitMultiSystem *sys, int n, int slices, bool f16
     stage = std::max(stage, t_stage(slices, m.No, false).bytes);
   }
   const size_t L3 = (size_t)no_lay * no_lay * no_lay;
-  const size_t fixed = 1024 + kTailBytes + staging_bytes_t(slices, no_lay) +
-                       sizeof(double) * 3 * (size_t)no_lay * no_lay;
+  const size_t fixed = 1024 + kTailBytes + staging_bytes_t(slices, no_lay);
   const bool wsmem = fixed + sizeof(double) * L3 + 3 * stage <= (size_t)kSmemLimit;
-  const size_t vfix = fixed + (wsmem ? sizeof(double) * L3 : 0);
+  size_t vfix = fixed + (wsmem ? sizeof(double) * L3 : 0);
+  const size_t vsm_bytes = sizeof(double) * 3 * (size_t)no_lay * no_lay;
+  const bool vsm = vfix + vsm_bytes + 3 * stage <= (size_t)kSmemLimit;
+  if (vsm) vfix += vsm_bytes;
   if (vfix >= (size_t)kSmemLimit) return ATRIP_ERR_UNSUPPORTED;
   int nst = (int)(((size_t)kSmemLimit - vfix) / stage);
   if (nst > kMaxStages) nst = kMaxStages;
@@ -1699,6 +1836,7 @@ int split_multi_prepare(const SplitMultiSystem *sys, int n, int slices, bool f16
   b.npass_lay = npass;
   b.nstages = nst;
   b.wsmem = wsmem ? 1 : 0;
+  b.vsm = vsm ? 1 : 0;
   b.stage_bytes = stage;
   b.smem = vfix + (size_t)nst * stage;
   return ATRIP_OK;
@@ -1733,6 +1871,7 @@ int split_multi_enqueue(const SplitMultiBuffers &b, double tai_sign, int sm_coun
   a.nsys = b.n;
   a.no_lay = b.no_lay;
   a.npass_lay = b.npass_lay;
+  a.vsm = b.vsm;
   const int grid = (int)std::min<int64_t>(total, sm_count);
   int rc;
   switch (b.slices) {
@@ -1742,6 +1881,17 @@ int split_multi_enqueue(const SplitMultiBuffers &b, double tai_sign, int sm_coun
   }
   if (rc != ATRIP_OK) return rc;
   *launches += 1;
+  return ATRIP_OK;
+}
+
+int split_profile_read(const SplitState &s, unsigned long long *out, int n) {
+  auto *p = static_cast<const SplitImpl *>(s.impl);
+  if (!p || !p->d_prof) {
+    set_error("split form: no profiled run on this context");
+    return ATRIP_ERR_STATE;
+  }
+  ATRIP_CUDA_TRY(cudaMemcpy(out, p->d_prof, sizeof(unsigned long long) * std::min(n, (int)kProfSlots),
+                            cudaMemcpyDeviceToHost));
   return ATRIP_OK;
 }
 
@@ -1831,9 +1981,17 @@ int split_enqueue(SplitState &s, const DeviceTensors &dt, int No, int Nv, int sm
   p->stage_cap = s.stage_cap;
   p->w_global = s.w_global;
   p->variant = s.variant;
-  ATRIP_CUDA_TRY(cudaMemsetAsync(p->wglobal, 0, sizeof(float) * need, st));
+  // no clearing of the W buffers: every cell a tuple's energy reads is
+  // stored by that tuple's groups before the energy warps get it
   ATRIP_CUDA_TRY(cudaMemsetAsync(p->d_status, 0, sizeof(int), st));
   SplitArgs a;
+  a.prof = nullptr;
+  if (s.profile) {
+    if (!p->d_prof)
+      ATRIP_CUDA_TRY(cudaMalloc(&p->d_prof, sizeof(unsigned long long) * kProfSlots));
+    ATRIP_CUDA_TRY(cudaMemsetAsync(p->d_prof, 0, sizeof(unsigned long long) * kProfSlots, st));
+    a.prof = p->d_prof;
+  }
   a.No = No;
   a.Nv = Nv;
   a.jt = 128 / No;

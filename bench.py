@@ -306,6 +306,37 @@ def _fp64_rate(ctx, n, fpt):
     return r.tuples_done * fpt / (r.device_ms * 1e-3) / 1e12, w
 
 
+def _role_profile(ctx, form, slices, lo, hi):
+    """One extra, untimed run of tuples [lo, hi) with the kernel built with
+    per-role cycle counters (atrip_gpu_split_profile; 2-slice transposed
+    kernel only): per role its cycles per tuple (one CTA) and the share of
+    its lifetime spent in each wait; the rest of a role's time is its work."""
+    from atrip_gb300 import capi
+    tuned = ctx.get_tuning()
+    try:
+        ctx.set_tuning(**dict(tuned, split_profile=1))
+        r = ctx.run(form=form, slices=slices, use_j=False, first_iteration=lo,
+                    max_iterations=hi - 1)
+        c = ctx.split_profile()
+    except capi.AtripError as exc:
+        return {"unavailable": str(exc)}
+    finally:
+        ctx.set_tuning(**tuned)
+    tuples = max(c["tuples"], 1)
+    roles = {"producer": ("stage", "tuple_slot"), "mma": ("tuple", "accumulator", "stage"),
+             "epilogue": ("tuple", "w_buffer", "accumulator"), "energy": ("tuple", "w")}
+    out = {"tuples": c["tuples"], "ctas": c["ctas"], "device_ms": r.device_ms,
+           "stages_per_tuple": c["stages"] / tuples,
+           "cycles_per_tuple": {k: c[f"{k}_total"] / tuples for k in roles},
+           "wait_share": {}}
+    for k, waits in roles.items():
+        tot = max(c[f"{k}_total"], 1)
+        for w in waits:
+            out["wait_share"][f"{k}_wait_{w}"] = c[f"{k}_wait_{w}"] / tot
+    out["wait_share"]["energy_w_convert"] = c["energy_w_convert"] / max(c["energy_total"], 1)
+    return out
+
+
 def _max_over_ranks(world, ms, count):
     if world <= 1:
         return ms, count
@@ -418,6 +449,11 @@ def run_single(args, workload, world, rank, local):
                                                     "sample_tuples")},
                    "tolerance_eh": args.tol_eh}
 
+    # ---- where the kernel's time goes: one untimed profiled run of a step
+    role_prof = None
+    if form != "fp64" and rank == 0 and not args.no_role_profile:
+        role_prof = _role_profile(ctx, form, slices, *stretch(0))
+
     # ---- end to end through the C ABI with host (pinned) buffers; the
     # timed context is released first so the large workloads fit twice over
     tuning_used = ctx.get_tuning()
@@ -483,6 +519,7 @@ def run_single(args, workload, world, rank, local):
                    "time_to_ET_s": time_to_et, "input_gen_s": t_gen},
         "compare_fp64": compare,
         "roofline": roof,
+        "role_profile": role_prof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": 16, "steps": e2e_steps,
@@ -719,6 +756,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-role-profile", action="store_true",
+                    help="skip the untimed profiled run behind role_profile")
     ap.add_argument("--whole-list-max-s", type=float, default=60.0,
                     help="run the end-to-end whole-list time to E(T) when the device rate "
                          "says it takes at most this long")

@@ -72,7 +72,7 @@ enum atrip_form {
                              /* given), FP64 for complex                      */
   ATRIP_FORM_SPLIT_F16 = 3   /* 2 FP16 slices of 11-bit digits (22 bits per  */
                              /* operand, the MMAs of 2 BF16 slices); level 0  */
-                             /* FP32-rounded; needs No <= 63 and              */
+                             /* FP32-rounded; needs No <= 64 and              */
                              /* 2 (Nv + No) < 2048                            */
 };
 
@@ -186,6 +186,9 @@ typedef struct {
   int32_t split_test_unpublished; /* test of that path: 1 = the kernel's producer */
                             /* publishes no tuple, so every other role's first    */
                             /* wait runs out (no copy or MMA is issued); 0 = off   */
+  int32_t split_profile;    /* split form: 1 = run the kernel built with per-role  */
+                            /* cycle counters (2 slices, transposed kernel only;   */
+                            /* same results), read by atrip_gpu_split_profile      */
 } atrip_tuning;
 
 /* Set / read the context's launch parameters (kept until changed). */
@@ -201,6 +204,22 @@ int atrip_gpu_get_tuning(const atrip_gpu_context *ctx, atrip_tuning *tuning);
  * (src/atrip/Atrip.cxx:1094-1107), without the rounding of one double per
  * process.                                                                 */
 int atrip_gpu_last_sums(const atrip_gpu_context *ctx, double *sums);
+
+/* Role profile of the last split-form run made with tuning split_profile = 1:
+ * SM cycles summed over the CTAs (clock64 on each role's leading thread),
+ *   [0] producer total      [1] producer waiting for a free ring stage
+ *   [2] producer waiting for a free tuple slot
+ *   [3] MMA issuer total    [4] ... waiting for a tuple   [5] ... for a free
+ *       accumulator          [6] ... for a filled ring stage
+ *   [7] epilogue total      [8] ... waiting for a tuple   [9] ... for a free
+ *       W buffer             [10] ... for a finished accumulator
+ *   [11] energy total       [12] ... waiting for a tuple  [13] ... for the
+ *       tuple's W            [14] ... converting W to FP64
+ *   [16] ring stages consumed  [17] tuples  [18] CTAs   (others 0)
+ * The reference's closest facility is its per-section Timings
+ * (src/atrip/Atrip.hpp:47); this one times the device roles instead. */
+#define ATRIP_SPLIT_PROFILE_COUNTERS 20
+int atrip_gpu_split_profile(const atrip_gpu_context *ctx, uint64_t *counters, int32_t n);
 
 /* Per-tuple energies of the last run, tuple-list positions t0 .. t0+n-1
  * (the sign atrip accumulates before its final negation). ect may be NULL. */

@@ -53,8 +53,9 @@ def test_split_formats_order_and_eligibility():
     assert autotune.split_formats(40, 400, "split_bf16") == [("split_bf16", 2), ("split_bf16", 3),
                                                              ("split_bf16", 4)]
     assert autotune.split_formats(40, 400, "split_f16") == [("split_f16", 2)]
-    # No > 63 (shared memory), or K = 2 (Nv + No) >= 2048: BF16 only
-    assert autotune.split_formats(64, 100)[0] == ("split_bf16", 2)
+    # No > 64 (2 No rows > 128), or K = 2 (Nv + No) >= 2048: BF16 only
+    assert autotune.split_formats(64, 100)[0] == ("split_f16", 2)
+    assert autotune.split_formats(65, 100)[0] == ("split_bf16", 2)
     assert autotune.split_formats(20, 1004)[0] == ("split_bf16", 2)
     assert autotune.f16_eligible(56, 560) and autotune.f16_eligible(63, 960)
     assert not autotune.f16_eligible(63, 961)
