@@ -203,6 +203,26 @@ def cpu_baseline_batch(ds, seconds=12.0, threads=None):
             "sample": "; ".join(parts) + f" ({secs:.1f} s)"}
 
 
+BATCH96 = "96 CCSD(T) triples systems, No in [4,20], Nv in [30,200], seeds 0..95"
+
+
+def workload_config(workload, No=None, Nv=None, n_tuples=None):
+    """The bench line's `config`: what identifies the workload, the same for
+    both arms (run-dependent details go to the line's `run` object)."""
+    from atrip_gb300 import capi, synth
+    if workload == "batch96":
+        n = sum(capi.n_tuples(nv) for _, nv, _ in synth.multi_system_sizes(96))
+        return {"workload": BATCH96, "name": "batch96", "n_tuples": n,
+                "l2": "no flush: inputs > 129 MB L2"}
+    # FP64 inputs: eps_i, eps_a, T1, T2, V_pphh, V_hhhp, V_pphp
+    nbytes = 8 * (No + Nv + Nv * No + 2 * Nv * Nv * No * No + No ** 3 * Nv + Nv ** 3 * No)
+    l2 = ("no flush: inputs > 129 MB L2" if nbytes > 129e6 else
+          f"no flush: the {nbytes / 1e6:.0f} MB of inputs fit the 129 MB L2 "
+          "(a parity-size workload, not a timing one)")
+    return {"workload": f"CCSD(T) triples No={No} Nv={Nv} seed {SEED}", "name": workload,
+            "n_tuples": n_tuples if n_tuples is not None else capi.n_tuples(Nv), "l2": l2}
+
+
 def run_reference_arm(args, workload):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -215,12 +235,12 @@ def run_reference_arm(args, workload):
         sizes = synth.multi_system_sizes(96)[::12]
         systems = [synth.make_inputs(No, Nv, s) for No, Nv, s in sizes]
         desc = "every 12th system of the 96-system workload"
-        wl = ("96 CCSD(T) triples systems, No in [4,20], Nv in [30,200], seeds 0..95")
+        cfg = workload_config("batch96")
     else:
         No, Nv = WORKLOADS[workload] if workload in WORKLOADS else (args.no, args.nv)
         systems = [synth.make_inputs(No, Nv, SEED)]
         desc = f"No={No} Nv={Nv} seed {SEED}"
-        wl = f"CCSD(T) triples No={No} Nv={Nv} seed {SEED}"
+        cfg = workload_config(workload, No, Nv)
     ports = [(d, oracle.PreparedPort(oracle.Problem(d)), int(oracle.n_tuples(d["Nv"])))
              for d in systems]
     times, flops = [], 0.0
@@ -245,9 +265,10 @@ def run_reference_arm(args, workload):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": wl, "name": workload, "systems": desc,
-                       "flops_per_step": flops / args.steps, "l2": "inputs > L2"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded, benchmark value distributions)",
+            "config": cfg,
+            "run": {"systems": desc, "flops_per_step": flops / args.steps},
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} steps of ~{args.ref_flops:.0e} FLOPs, "
                                        f"stretches from the middle of the tuple list ({desc})"},
@@ -512,11 +533,10 @@ def run_single(args, workload, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if form == "fp64" else f"{form[6:]}x{slices}->f64",
         "data": "synthetic (seeded, benchmark value distributions)",
-        "config": {"workload": f"CCSD(T) triples No={No} Nv={Nv} seed {SEED}", "name": workload,
-                   "form": form, "slices": slices, "tuning": tune["tuning"],
-                   "tuples_per_step": batch, "stretches": parts, "n_tuples": n,
-                   "l2": "no flush: inputs > 129 MB L2",
-                   "time_to_ET_s": time_to_et, "input_gen_s": t_gen},
+        "config": workload_config(workload, No, Nv, n),
+        "run": {"form": form, "slices": slices, "tuning": tune["tuning"],
+                "tuples_per_step": batch, "stretches": parts,
+                "time_to_ET_s": time_to_et, "input_gen_s": t_gen},
         "compare_fp64": compare,
         "roofline": roof,
         "role_profile": role_prof,
@@ -645,16 +665,15 @@ def run_batch96(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if form == "fp64" else f"{form[6:]}x{slices}->f64",
         "data": "synthetic (seeded, benchmark value distributions)",
-        "config": {"workload": "96 CCSD(T) triples systems, No in [4,20], Nv in [30,200], "
-                               "seeds 0..95", "name": "batch96", "form": form, "slices": slices,
-                   "tuples_per_step": total_tuples, "flops_per_step": total_flops,
-                   "fp64_row_tiles": {"32": tiles.count(32), "64": tiles.count(64)},
-                   "batch_tuning": btune["tuning"],
-                   "split_tuning": split_choice[1] if split_choice else None,
-                   "split_trials_ms": [(round(t, 2), c) for t, c in trials] if split_choice
-                   else None,
-                   "l2": "no flush: inputs > 129 MB L2",
-                   "time_to_ET_s": ms / args.steps / 1e3, "input_gen_s": t_gen},
+        "config": workload_config("batch96"),
+        "run": {"form": form, "slices": slices,
+                "tuples_per_step": total_tuples, "flops_per_step": total_flops,
+                "fp64_row_tiles": {"32": tiles.count(32), "64": tiles.count(64)},
+                "batch_tuning": btune["tuning"],
+                "split_tuning": split_choice[1] if split_choice else None,
+                "split_trials_ms": [(round(t, 2), c) for t, c in trials] if split_choice
+                else None,
+                "time_to_ET_s": ms / args.steps / 1e3, "input_gen_s": t_gen},
         "compare_fp64": compare,
         "roofline": roof,
         "cpu_baseline": cpu,
