@@ -71,3 +71,34 @@ def test_batch_plan_orders_by_cost():
     assert lib.atrip_gpu_batch_plan(None, None, 3, None) == capi.ERR_ARGUMENT
     h = ctypes.c_void_p()
     assert lib.atrip_gpu_batch_create(None, 0, ctypes.byref(h)) == capi.ERR_ARGUMENT
+
+
+def test_split_profile_counter_layout_matches_kernel_and_header():
+    """capi.SPLIT_PROFILE (the Python names of atrip_gpu_split_profile's
+    counters) follows the kernel's slot enum and the header's count."""
+    src = open(os.path.join(ROOT, "atrip_gb300", "csrc", "split_bf16.cu")).read()
+    body = re.search(r"enum ProfSlot \{(.*?)\};", src, re.S).group(1)
+    slots, nxt = {}, 0
+    for item in (x.strip() for x in body.split(",")):
+        if not item:
+            continue
+        name, _, val = (p.strip() for p in item.partition("="))
+        nxt = int(val) if val else nxt
+        slots[name] = nxt
+        nxt += 1
+    hdr = open(os.path.join(ROOT, "include", "atrip_gb300.h")).read()
+    count = int(re.search(r"#define ATRIP_SPLIT_PROFILE_COUNTERS (\d+)", hdr).group(1))
+    assert slots["kProfSlots"] == count == capi.SPLIT_PROFILE_COUNTERS
+    kernel_names = {
+        "kProfProdTotal": "producer_total", "kProfProdEmpty": "producer_wait_stage",
+        "kProfProdTupleEmpty": "producer_wait_tuple_slot", "kProfMmaTotal": "mma_total",
+        "kProfMmaTupleFull": "mma_wait_tuple", "kProfMmaAccEmpty": "mma_wait_accumulator",
+        "kProfMmaFull": "mma_wait_stage", "kProfEpiTotal": "epilogue_total",
+        "kProfEpiTupleFull": "epilogue_wait_tuple", "kProfEpiWFree": "epilogue_wait_w_buffer",
+        "kProfEpiAccFull": "epilogue_wait_accumulator", "kProfEnTotal": "energy_total",
+        "kProfEnTupleFull": "energy_wait_tuple", "kProfEnWFull": "energy_wait_w",
+        "kProfEnWConvert": "energy_w_convert", "kProfUnits": "stages",
+        "kProfTuples": "tuples", "kProfCtas": "ctas"}
+    for k, py in kernel_names.items():
+        assert capi.SPLIT_PROFILE[slots[k]] == py, (k, slots[k])
+    assert len(kernel_names) == len([n for n in capi.SPLIT_PROFILE if n])
